@@ -1,0 +1,852 @@
+// blamm_gpu.cu -- libblamm_gpu.so: the C ABI declared in include/blamm_gpu.h.
+//
+// Host half of the GB300 scan: motif-bank planning (length-sorted N tiles,
+// fixed-point BF16 hi/lo split, per-column guard band), device buffers, and
+// the drivers that chain pack -> fused tcgen05 scan -> FP32 rescoring (or the
+// plain FP32 kernel) on the context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/blamm_gpu.h"
+#include "scan_kernels.cuh"
+
+using namespace blamm;
+
+static_assert(sizeof(blamm_hit) == sizeof(HitRec), "hit record layout");
+
+struct blamm_ctx {
+    int device = 0;
+    int sm_count = 0;
+    int max_smem = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string err;
+    int mode = BLAMM_MODE_BF16X2;
+    int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
+    long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
+
+    // motif bank (host copy)
+    int ncols = 0, p_rows = 0, lmax = 0;
+    std::vector<float> P;
+    std::vector<int32_t> len;
+    std::vector<float> thr;
+    float *d_P = nullptr;
+    int32_t *d_len = nullptr;
+    float *d_thr = nullptr;
+
+    // tensor-core plan (valid for plan_terms; rebuilt on mode/threshold change)
+    int plan_terms = 0;
+    bool plan_valid = false;
+    std::vector<TileDesc> tiles;
+    std::vector<float> guard;  // per column
+    int nslots = 0, wrows = 0;
+    uint32_t b_term_max = 0, tmem_cols = 0;
+    TileDesc *d_tiles = nullptr;
+    uint8_t *d_bbuf = nullptr;
+    float *d_thr_adj = nullptr;
+    int32_t *d_slot_col = nullptr;
+
+    // stream buffers
+    char *d_bases = nullptr;
+    size_t cap_bases = 0;
+    uint32_t *d_seq2 = nullptr, *d_zmask = nullptr;
+    size_t cap_words32 = 0, cap_zmask = 0;
+    int64_t *d_runs = nullptr;
+    size_t cap_runs = 0;
+    unsigned long long *d_cand = nullptr;
+    int64_t cand_cap = 0;
+    blamm_hit *d_hits = nullptr;
+    int64_t hits_cap = 0;
+    unsigned long long *d_counters = nullptr;  // [0] candidates, [1] hits
+    int *d_status = nullptr;
+
+    blamm_stats stats{};
+};
+
+// ------------------------------------------------------------------ errors
+static int fail(blamm_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? BLAMM_ERR_NOMEM : BLAMM_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+template <typename T>
+static int ensure(blamm_ctx *ctx, T **ptr, size_t *cap, size_t need)
+{
+    if (need <= *cap && *ptr) return BLAMM_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    size_t n = std::max<size_t>(need, 1);
+    CK(cudaMalloc((void **)ptr, n * sizeof(T)));
+    *cap = n;
+    return BLAMM_OK;
+}
+
+// ------------------------------------------------------------------ planning
+namespace {
+
+// Fixed-point BF16 split of one column: hi on the grid 2^-k, lo on 2^-(k+8),
+// with k chosen so |hi| <= 128 * 2^-k.  Every partial sum of such values over
+// up to 256 motif positions is an integer multiple of 2^-(k+8) below 2^24 of
+// those units, i.e. exactly representable in FP32: the tensor-core
+// accumulation is exact, whatever its internal rounding.
+struct ColQuant {
+    int k;
+};
+
+int column_exponent(const float *col, int L)
+{
+    double mx = 0.0;
+    for (int r = 0; r < 4 * L; ++r) mx = std::max(mx, (double)std::fabs(col[r]));
+    if (!(mx > 0.0) || !std::isfinite(mx)) return -30;
+    int e;
+    double f = std::frexp(mx, &e);  // mx = f * 2^e, f in [0.5, 1)
+    if (f == 0.5) e -= 1;           // mx is a power of two: mx <= 2^(e-1)
+    return std::max(-30, std::min(40, e));
+}
+
+inline double q_hi(double v, int k) { return std::nearbyint(std::ldexp(v, k)) * std::ldexp(1.0, -k); }
+inline double q_lo(double r, int k) { return std::nearbyint(std::ldexp(r, k + 8)) * std::ldexp(1.0, -(k + 8)); }
+
+inline uint16_t bf16_bits_exact(double v)
+{
+    float f = (float)v;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (uint16_t)(u >> 16);  // exact: v has <= 8 significant bits
+}
+
+float round_down_float(double t)
+{
+    if (std::isnan(t)) return std::numeric_limits<float>::infinity();
+    float f = (float)t;
+    if ((double)f > t) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+
+}  // namespace
+
+static int build_plan(blamm_ctx *ctx, int terms)
+{
+    const int ncols = ctx->ncols;
+    if (ctx->lmax > kMaxTcLen)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED,
+                    "motif length %d exceeds the tensor-core limit %d (use BLAMM_MODE_FP32)",
+                    ctx->lmax, kMaxTcLen);
+    // columns sorted by length (the reference's order already is, fwd/rc interleaved)
+    std::vector<int> order(ncols);
+    for (int i = 0; i < ncols; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return ctx->len[a] < ctx->len[b]; });
+
+    const int gmax_all = std::max(1, (ctx->lmax + 3) / 4);
+    const int wrows_all = kBM + 8 * (((gmax_all + 1) / 2) - 1);
+    const long long smem_limit = (long long)ctx->max_smem;
+    const long long other = 2LL * wrows_all * kWRowBytes + (long long)(ncols + 32 * (ncols / 32 + 16)) * 4 +
+                            4LL * kCandBuf * 8 + wrows_all + 64 + 64LL * sizeof(TileDesc) + 400 + 256 +
+                            2048;
+    const long long b_term_cap = (smem_limit - other) / terms;
+    auto nmax_for = [&](int g) {
+        long long n = b_term_cap / (32LL * g);
+        n = n / 32 * 32;
+        return (int)std::min<long long>(256, n);
+    };
+    if (nmax_for(gmax_all) < 32)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "motif bank does not fit shared memory");
+
+    // DP over sorted columns: tile = contiguous run of sorted columns.
+    // Per-job cycle model: MMA = terms*g*N/2, epilogue ~ 2.5*N, W build ~ 300,
+    // fixed overhead ~ 150.
+    const double kInf = 1e300;
+    std::vector<double> f(ncols + 1, kInf);
+    std::vector<int> from(ncols + 1, -1);
+    f[0] = 0.0;
+    for (int j = 1; j <= ncols; ++j) {
+        for (int i = j - 1; i >= 0 && j - i <= 256; --i) {
+            const int L = ctx->len[order[j - 1]];
+            const int g = std::max(1, (L + 3) / 4);
+            const int N = (j - i + 31) / 32 * 32;
+            if (N > nmax_for(g)) break;
+            const double mma = terms * g * N / 2.0, epi = 2.5 * N;
+            const double cost = std::max(std::max(mma, epi), 300.0) + 150.0;
+            if (f[i] + cost < f[j]) {
+                f[j] = f[i] + cost;
+                from[j] = i;
+            }
+        }
+        if (from[j] < 0) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "tile planning failed");
+    }
+    std::vector<std::pair<int, int>> spans;
+    for (int j = ncols; j > 0; j = from[j]) spans.push_back({from[j], j});
+    std::reverse(spans.begin(), spans.end());
+
+    // per-column quantisation and guard band
+    std::vector<int> kcol(ncols);
+    ctx->guard.assign(ncols, 0.0f);
+    std::vector<double> guard_d(ncols, 0.0);
+    for (int c = 0; c < ncols; ++c) {
+        const float *col = &ctx->P[(size_t)c * ctx->p_rows];
+        const int L = ctx->len[c];
+        const int k = 7 - column_exponent(col, L);
+        kcol[c] = k;
+        double eq = 0.0, a = 0.0;
+        for (int j = 0; j < L; ++j) {
+            double mres = 0.0, mabs = 0.0;
+            for (int b = 0; b < 4; ++b) {
+                const double v = col[4 * j + b];
+                const double hi = q_hi(v, k);
+                const double lo = terms == 2 ? q_lo(v - hi, k) : 0.0;
+                mres = std::max(mres, std::fabs(v - hi - lo));
+                mabs = std::max(mabs, std::fabs(v));
+            }
+            eq += mres;
+            a += mabs;
+        }
+        // |fl(sequential sum) - exact sum| <= gamma_{L-1} * sum|terms|
+        const double u = std::ldexp(1.0, -24);
+        const double nl = std::max(0, L - 1);
+        const double gamma = nl * u / (1.0 - nl * u);
+        guard_d[c] = (eq + gamma * a) * (1.0 + 1e-9) + std::ldexp(1.0, -60);
+        ctx->guard[c] = (float)guard_d[c];
+    }
+
+    // tiles, slots, B buffer
+    std::vector<TileDesc> tiles;
+    std::vector<float> thr_adj;
+    std::vector<int32_t> slot_col;
+    std::vector<uint8_t> bbuf;
+    int gmax = 1;
+    uint32_t btmax = 0;
+    int nmax = 0;
+    for (auto &sp : spans) {
+        const int cnt = sp.second - sp.first;
+        const int L = ctx->len[order[sp.second - 1]];
+        const int g = std::max(1, (L + 3) / 4);
+        const int N = (cnt + 31) / 32 * 32;
+        TileDesc td{};
+        td.slot0 = (int32_t)slot_col.size();
+        td.n = N;
+        td.g = g;
+        td.b_bytes = N * 16 * g * 2;
+        size_t off = (bbuf.size() + 1023) / 1024 * 1024;
+        td.b_off = (int64_t)off;
+        bbuf.resize(off + (size_t)td.b_bytes * terms, 0);
+        for (int i = 0; i < N; ++i) {
+            const int c = i < cnt ? order[sp.first + i] : -1;
+            slot_col.push_back(c);
+            if (c < 0) {
+                thr_adj.push_back(std::numeric_limits<float>::infinity());
+                continue;
+            }
+            thr_adj.push_back(round_down_float((double)ctx->thr[c] - guard_d[c]));
+            const float *col = &ctx->P[(size_t)c * ctx->p_rows];
+            const int Lc = ctx->len[c];
+            const int ng = i / 8, r = i % 8;
+            for (int kk = 0; kk < 16 * g; ++kk) {
+                const int j = kk / 4;
+                if (j >= Lc) break;
+                const double v = col[kk];
+                const double hi = q_hi(v, kcol[c]);
+                const double lo = q_lo(v - hi, kcol[c]);
+                const int kc = kk / 8, e = kk % 8;
+                const size_t elem = ((size_t)(ng * 2 * g + kc) * 8 + r) * 8 + e;
+                uint16_t *b_hi = reinterpret_cast<uint16_t *>(bbuf.data() + off);
+                b_hi[elem] = bf16_bits_exact(hi);
+                if (terms == 2) {
+                    uint16_t *b_lo = reinterpret_cast<uint16_t *>(bbuf.data() + off + td.b_bytes);
+                    b_lo[elem] = bf16_bits_exact(lo);
+                }
+            }
+        }
+        tiles.push_back(td);
+        gmax = std::max(gmax, g);
+        btmax = std::max<uint32_t>(btmax, (uint32_t)td.b_bytes);
+        nmax = std::max(nmax, N);
+    }
+
+    // upload
+    if (ctx->d_tiles) cudaFree(ctx->d_tiles);
+    if (ctx->d_bbuf) cudaFree(ctx->d_bbuf);
+    if (ctx->d_thr_adj) cudaFree(ctx->d_thr_adj);
+    if (ctx->d_slot_col) cudaFree(ctx->d_slot_col);
+    ctx->d_tiles = nullptr;
+    ctx->d_bbuf = nullptr;
+    ctx->d_thr_adj = nullptr;
+    ctx->d_slot_col = nullptr;
+    CK(cudaMalloc(&ctx->d_tiles, sizeof(TileDesc) * tiles.size()));
+    CK(cudaMalloc(&ctx->d_bbuf, bbuf.size()));
+    CK(cudaMalloc(&ctx->d_thr_adj, sizeof(float) * thr_adj.size()));
+    CK(cudaMalloc(&ctx->d_slot_col, sizeof(int32_t) * slot_col.size()));
+    CK(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_bbuf, bbuf.data(), bbuf.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_thr_adj, thr_adj.data(), sizeof(float) * thr_adj.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_slot_col, slot_col.data(), sizeof(int32_t) * slot_col.size(), cudaMemcpyHostToDevice));
+    ctx->tiles = tiles;
+    ctx->nslots = (int)slot_col.size();
+    ctx->wrows = kBM + 8 * (((gmax + 1) / 2) - 1);
+    ctx->b_term_max = btmax;
+    ctx->tmem_cols = nmax <= 128 ? 256u : 512u;
+    ctx->plan_terms = terms;
+    ctx->plan_valid = true;
+    return BLAMM_OK;
+}
+
+// ------------------------------------------------------------------ API
+extern "C" {
+
+int blamm_version(void) { return 10000; }
+
+int blamm_ctx_create(int device, blamm_ctx **out)
+{
+    if (!out) return BLAMM_ERR_ARG;
+    *out = nullptr;
+    blamm_ctx *ctx = new blamm_ctx();
+    ctx->device = device;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || device < 0 || device >= ndev) {
+        delete ctx;
+        return BLAMM_ERR_CUDA;
+    }
+    int rc = BLAMM_OK;
+    auto init = [&]() -> int {
+        CK(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, device));
+        if (prop.major != 10)
+            return fail(ctx, BLAMM_ERR_UNSUPPORTED, "compute capability %d.%d is not sm_100-class",
+                        prop.major, prop.minor);
+        ctx->sm_count = prop.multiProcessorCount;
+        ctx->max_smem = (int)prop.sharedMemPerBlockOptin;
+        cudaFuncAttributes fa;
+        CK(cudaFuncGetAttributes(&fa, scan_tc_kernel));  // fails if no sm_103a image fits
+        CK(cudaFuncSetAttribute(scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                ctx->max_smem));
+        CK(cudaFuncSetAttribute(scan_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                ctx->max_smem));
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        for (auto &ev : ctx->ev) CK(cudaEventCreate(&ev));
+        CK(cudaMalloc(&ctx->d_counters, 4 * sizeof(unsigned long long)));
+        CK(cudaMalloc(&ctx->d_status, sizeof(int)));
+        return BLAMM_OK;
+    };
+    rc = init();
+    if (rc != BLAMM_OK) {
+        fprintf(stderr, "blamm_ctx_create: %s\n", ctx->err.c_str());
+        blamm_ctx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return BLAMM_OK;
+}
+
+void blamm_ctx_destroy(blamm_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    void *bufs[] = {ctx->d_P,      ctx->d_len,   ctx->d_thr,      ctx->d_tiles, ctx->d_bbuf,
+                    ctx->d_thr_adj, ctx->d_slot_col, ctx->d_bases, ctx->d_seq2, ctx->d_zmask,
+                    ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *blamm_last_error(const blamm_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int blamm_set_mode(blamm_ctx *ctx, int mode)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    if (mode != BLAMM_MODE_FP32 && mode != BLAMM_MODE_BF16 && mode != BLAMM_MODE_BF16X2)
+        return fail(ctx, BLAMM_ERR_ARG, "unknown mode %d", mode);
+    ctx->mode = mode;
+    return BLAMM_OK;
+}
+
+int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols, const int32_t *col_len,
+                     const float *thr)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    if (!P || !col_len || !thr || ncols <= 0 || p_rows <= 0 || p_rows % 4)
+        return fail(ctx, BLAMM_ERR_ARG, "invalid motif bank arguments");
+    if (ncols >= (1 << kColBits)) return fail(ctx, BLAMM_ERR_ARG, "too many motif columns");
+    int lmax = 0;
+    for (int c = 0; c < ncols; ++c) {
+        if (col_len[c] <= 0 || 4 * col_len[c] > p_rows)
+            return fail(ctx, BLAMM_ERR_ARG, "column %d: length %d does not fit %d rows", c, col_len[c],
+                        p_rows);
+        lmax = std::max(lmax, (int)col_len[c]);
+    }
+    CK(cudaSetDevice(ctx->device));
+    ctx->ncols = ncols;
+    ctx->p_rows = p_rows;
+    ctx->lmax = lmax;
+    ctx->P.assign(P, P + (size_t)p_rows * ncols);
+    ctx->len.assign(col_len, col_len + ncols);
+    ctx->thr.assign(thr, thr + ncols);
+    if (ctx->d_P) cudaFree(ctx->d_P);
+    if (ctx->d_len) cudaFree(ctx->d_len);
+    if (ctx->d_thr) cudaFree(ctx->d_thr);
+    ctx->d_P = nullptr;
+    ctx->d_len = nullptr;
+    ctx->d_thr = nullptr;
+    CK(cudaMalloc(&ctx->d_P, sizeof(float) * ctx->P.size()));
+    CK(cudaMalloc(&ctx->d_len, sizeof(int32_t) * ncols));
+    CK(cudaMalloc(&ctx->d_thr, sizeof(float) * ncols));
+    CK(cudaMemcpy(ctx->d_P, ctx->P.data(), sizeof(float) * ctx->P.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_len, ctx->len.data(), sizeof(int32_t) * ncols, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_thr, ctx->thr.data(), sizeof(float) * ncols, cudaMemcpyHostToDevice));
+    ctx->plan_valid = false;
+    return BLAMM_OK;
+}
+
+int blamm_set_thresholds(blamm_ctx *ctx, const float *thr)
+{
+    if (!ctx || !thr) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    CK(cudaSetDevice(ctx->device));
+    ctx->thr.assign(thr, thr + ctx->ncols);
+    CK(cudaMemcpy(ctx->d_thr, ctx->thr.data(), sizeof(float) * ctx->ncols, cudaMemcpyHostToDevice));
+    ctx->plan_valid = false;
+    return BLAMM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ drivers
+static int ensure_plan(blamm_ctx *ctx)
+{
+    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    if (ctx->plan_valid && ctx->plan_terms == terms) return BLAMM_OK;
+    return build_plan(ctx, terms);
+}
+
+static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
+{
+    const int64_t nwords32 = (n + kStreamPad + 31) / 32;
+    int rc = ensure(ctx, &ctx->d_seq2, &ctx->cap_words32, (size_t)(2 * nwords32));
+    if (rc) return rc;
+    rc = ensure(ctx, &ctx->d_zmask, &ctx->cap_zmask, (size_t)nwords32);
+    if (rc) return rc;
+    const int threads = 256;
+    const int64_t blocks = (nwords32 + threads - 1) / threads;
+    pack_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
+                                                               nwords32, ctx->lower_scores);
+    CK(cudaGetLastError());
+    return BLAMM_OK;
+}
+
+// tcgen05 scan + rescoring; candidates buffer grows (and the scan re-runs) on overflow
+static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
+                  int64_t hit_cap, float *dump, int64_t dump_p0, int64_t dump_npos, int *launches)
+{
+    int rc = ensure_plan(ctx);
+    if (rc) return rc;
+    const int64_t n_mtiles = (n + kBM - 1) / kBM;
+    const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    if (ctx->cand_cap == 0) {
+        const double est = (double)n * ctx->ncols / 1000.0;
+        int64_t want = (int64_t)std::min(std::max(est, (double)(1 << 20)), 512.0 * 1024 * 1024);
+        size_t cap = 0;
+        rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)want);
+        if (rc) return rc;
+        ctx->cand_cap = (int64_t)cap;
+    }
+    const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->wrows, ctx->nslots,
+                                    (int)ctx->tiles.size());
+    if ((int)L.total > ctx->max_smem)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
+    // at least ~116 KB so that two CTAs never share an SM (each allocates TMEM)
+    const uint32_t smem = std::max<uint32_t>(L.total, 116 * 1024);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        TcParams p{};
+        p.seq2 = ctx->d_seq2;
+        p.zmask = ctx->d_zmask;
+        p.n = n;
+        p.n_mtiles = n_mtiles;
+        p.tiles = ctx->d_tiles;
+        p.ntiles = (int32_t)ctx->tiles.size();
+        p.terms = ctx->plan_terms;
+        p.bbuf = ctx->d_bbuf;
+        p.thr_adj = ctx->d_thr_adj;
+        p.slot_col = ctx->d_slot_col;
+        p.nslots = ctx->nslots;
+        p.wrows = ctx->wrows;
+        p.b_term_max = ctx->b_term_max;
+        p.tmem_cols = ctx->tmem_cols;
+        p.cand = ctx->d_cand;
+        p.cand_count = ctx->d_counters;
+        p.cand_cap = ctx->cand_cap;
+        p.status = ctx->d_status;
+        p.wait_limit = ctx->wait_limit;
+        p.dump = dump;
+        p.dump_p0 = dump_p0;
+        p.dump_npos = dump_npos;
+        p.dump_ncols = ctx->ncols;
+        const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
+        if (njobs > 0) {
+            scan_tc_kernel<<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            CK(cudaGetLastError());
+            ++*launches;
+        }
+        unsigned long long ncand = 0;
+        int status = 0;
+        CK(cudaMemcpyAsync(&ncand, ctx->d_counters, sizeof ncand, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (status) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
+        ctx->stats.candidates = (int64_t)ncand;
+        if ((int64_t)ncand <= ctx->cand_cap) break;
+        // grow and re-run
+        size_t cap = 0;
+        cudaFree(ctx->d_cand);
+        ctx->d_cand = nullptr;
+        ctx->cand_cap = 0;
+        rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)(ncand + ncand / 4 + 1024));
+        if (rc) return rc;
+        ctx->cand_cap = (int64_t)cap;
+        if (attempt == 2) return fail(ctx, BLAMM_ERR_OVERFLOW, "candidate buffer overflow");
+    }
+    RescoreParams r{};
+    r.cand = ctx->d_cand;
+    r.cand_count = ctx->d_counters;
+    r.cand_cap = ctx->cand_cap;
+    r.seq2 = ctx->d_seq2;
+    r.zmask = ctx->d_zmask;
+    r.n = n;
+    r.run_start = d_runs;
+    r.nruns = nruns;
+    r.P = ctx->d_P;
+    r.p_rows = ctx->p_rows;
+    r.col_len = ctx->d_len;
+    r.thr = ctx->d_thr;
+    r.hits = d_hits;
+    r.hit_count = ctx->d_counters + 1;
+    r.hit_cap = hit_cap;
+    const int64_t nc = ctx->stats.candidates;
+    if (nc > 0) {
+        const int threads = 256;
+        const int64_t blocks = std::min<int64_t>((nc + threads - 1) / threads, (int64_t)ctx->sm_count * 16);
+        rescore_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(r);
+        CK(cudaGetLastError());
+        ++*launches;
+    }
+    return BLAMM_OK;
+}
+
+static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
+                     int64_t hit_cap, int *launches)
+{
+    CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    PlainParams p{};
+    p.seq2 = ctx->d_seq2;
+    p.zmask = ctx->d_zmask;
+    p.n = n;
+    p.run_start = d_runs;
+    p.nruns = nruns;
+    p.P = ctx->d_P;
+    p.p_rows = ctx->p_rows;
+    p.ncols = ctx->ncols;
+    p.lmax = ctx->lmax;
+    p.col_len = ctx->d_len;
+    p.thr = ctx->d_thr;
+    p.hits = d_hits;
+    p.hit_count = ctx->d_counters + 1;
+    p.hit_cap = hit_cap;
+    const int threads = 256;
+    int cpb = 32;
+    while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
+    p.cols_per_block = cpb;
+    const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
+    const int64_t bx = (n + threads - 1) / threads;
+    const int by = (ctx->ncols + cpb - 1) / cpb;
+    if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
+    if (bx > 0) {
+        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
+        CK(cudaGetLastError());
+        ++*launches;
+    }
+    return BLAMM_OK;
+}
+
+static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_runs, int64_t nruns,
+                     blamm_hit *d_hits, int64_t hit_cap, int64_t *n_hits)
+{
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    int launches = 0;
+    ctx->stats = blamm_stats{};
+    ctx->stats.positions = n;
+    ctx->stats.columns = ctx->ncols;
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    int rc = launch_pack(ctx, d_bases, n);
+    if (rc) return rc;
+    ++launches;
+    if (ctx->mode == BLAMM_MODE_FP32) rc = run_plain(ctx, n, d_runs, nruns, d_hits, hit_cap, &launches);
+    else rc = run_tc(ctx, n, d_runs, nruns, d_hits, hit_cap, nullptr, 0, 0, &launches);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    unsigned long long nh = 0;
+    CK(cudaMemcpyAsync(&nh, ctx->d_counters + 1, sizeof nh, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.hits = (int64_t)nh;
+    ctx->stats.tiles = (int32_t)(ctx->mode == BLAMM_MODE_FP32 ? 0 : ctx->tiles.size());
+    ctx->stats.launches = launches;
+    *n_hits = (int64_t)nh;
+    return (int64_t)nh > hit_cap ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld",
+                                        (long long)nh, (long long)hit_cap)
+                                 : BLAMM_OK;
+}
+
+extern "C" {
+
+int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
+                      int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, int64_t *n_hits)
+{
+    if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
+    *n_hits = 0;
+    if (n == 0) return BLAMM_OK;
+    if (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits))
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    return scan_core(ctx, d_bases, n, d_run_start, nruns, d_hits, hit_cap, n_hits);
+}
+
+int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start, int64_t nruns,
+               blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
+{
+    if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
+    *n_hits = 0;
+    if (n == 0) return BLAMM_OK;
+    if (!bases || !run_start || nruns <= 0 || (hit_cap > 0 && !hits))
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    if (run_start[0] != 0) return fail(ctx, BLAMM_ERR_ARG, "run_start[0] must be 0");
+    for (int64_t r = 1; r < nruns; ++r)
+        if (run_start[r] <= run_start[r - 1] || run_start[r] >= n)
+            return fail(ctx, BLAMM_ERR_ARG, "run_start must ascend strictly inside [0, n)");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
+    if (rc) return rc;
+    rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, (size_t)nruns);
+    if (rc) return rc;
+    size_t hc = (size_t)ctx->hits_cap;
+    rc = ensure(ctx, &ctx->d_hits, &hc, (size_t)std::max<int64_t>(hit_cap, 1));
+    if (rc) return rc;
+    ctx->hits_cap = (int64_t)hc;
+    CK(cudaMemcpyAsync(ctx->d_bases, bases, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_runs, run_start, sizeof(int64_t) * nruns, cudaMemcpyHostToDevice, ctx->stream));
+    rc = scan_core(ctx, ctx->d_bases, n, ctx->d_runs, nruns, ctx->d_hits, hit_cap, n_hits);
+    if (rc && rc != BLAMM_ERR_OVERFLOW) return rc;
+    const int64_t ncopy = std::min<int64_t>(*n_hits, hit_cap);
+    if (ncopy > 0)
+        CK(cudaMemcpyAsync(hits, ctx->d_hits, sizeof(blamm_hit) * ncopy, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]);
+    ctx->stats.total_ms = ms;
+    return rc;
+}
+
+int blamm_filter_score(blamm_ctx *ctx, float *d_R, int m, int n, const float *d_threshold, int *d_occIdx,
+                       float *d_occScore, int *d_nOcc)
+{
+    if (!ctx || m < 0 || n < 0) return BLAMM_ERR_ARG;
+    if ((long long)m * n == 0) return BLAMM_OK;
+    if (!d_R || !d_threshold || !d_occIdx || !d_occScore || !d_nOcc)
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    const long long total = (long long)m * n;
+    const int threads = 256;
+    const long long blocks = std::min<long long>((total + threads - 1) / threads, (long long)ctx->sm_count * 32);
+    filter_score_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(d_R, m, n, d_threshold, d_occIdx,
+                                                                      d_occScore, d_nOcc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BLAMM_OK;
+}
+
+int blamm_device_count(int *n)
+{
+    if (!n) return BLAMM_ERR_ARG;
+    *n = 0;
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return BLAMM_OK;
+    }
+    *n = c;
+    return BLAMM_OK;
+}
+
+int blamm_set_softmask(blamm_ctx *ctx, int lowercase_scores)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    ctx->lower_scores = lowercase_scores ? 1 : 0;
+    return BLAMM_OK;
+}
+
+int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                           int64_t nruns, const float *min_score, const float *width, int nbins,
+                           uint64_t *counts)
+{
+    if (!ctx || n < 0 || nbins <= 0 || !min_score || !width || !counts) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    if (n == 0) return BLAMM_OK;
+    if (!bases || !run_start || nruns <= 0) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
+    if (rc) return rc;
+    rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, (size_t)nruns);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_bases, bases, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_runs, run_start, sizeof(int64_t) * nruns, cudaMemcpyHostToDevice, ctx->stream));
+    rc = launch_pack(ctx, ctx->d_bases, n);
+    if (rc) return rc;
+    const size_t nc = (size_t)ctx->ncols;
+    float *d_min = nullptr, *d_w = nullptr;
+    unsigned long long *d_counts = nullptr;
+    auto cleanup = [&]() {
+        if (d_min) cudaFree(d_min);
+        if (d_w) cudaFree(d_w);
+        if (d_counts) cudaFree(d_counts);
+    };
+    cudaError_t e = cudaMalloc(&d_min, sizeof(float) * nc);
+    if (e == cudaSuccess) e = cudaMalloc(&d_w, sizeof(float) * nc);
+    if (e == cudaSuccess) e = cudaMalloc(&d_counts, sizeof(unsigned long long) * nc * nbins);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_min, min_score, sizeof(float) * nc, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, width, sizeof(float) * nc, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_counts, 0, sizeof(unsigned long long) * nc * nbins, ctx->stream);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
+    }
+    HistParams p{};
+    p.seq2 = ctx->d_seq2;
+    p.zmask = ctx->d_zmask;
+    p.n = n;
+    p.run_start = ctx->d_runs;
+    p.nruns = nruns;
+    p.P = ctx->d_P;
+    p.p_rows = ctx->p_rows;
+    p.ncols = ctx->ncols;
+    p.lmax = ctx->lmax;
+    p.col_len = ctx->d_len;
+    p.min_score = d_min;
+    p.width = d_w;
+    p.nbins = nbins;
+    p.counts = d_counts;
+    const int threads = 256;
+    int cpb = 32;
+    auto need = [&](int c) { return (size_t)c * (p.p_rows + nbins) * 4 + threads + p.lmax + 64; };
+    while (cpb > 1 && need(cpb) > (size_t)ctx->max_smem) cpb /= 2;
+    if (need(cpb) > (size_t)ctx->max_smem) {
+        cleanup();
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "too many bins for shared memory");
+    }
+    p.cols_per_block = cpb;
+    const int64_t bx = (n + threads - 1) / threads;
+    const int by = (ctx->ncols + cpb - 1) / cpb;
+    e = cudaFuncSetAttribute(score_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->max_smem);
+    if (e == cudaSuccess) {
+        score_hist_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, need(cpb), ctx->stream>>>(p);
+        e = cudaGetLastError();
+    }
+    std::vector<unsigned long long> host(nc * nbins);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host.data(), d_counts, sizeof(unsigned long long) * nc * nbins, cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
+    for (size_t i = 0; i < nc * (size_t)nbins; ++i) counts[i] += host[i];
+    return BLAMM_OK;
+}
+
+int blamm_last_stats(const blamm_ctx *ctx, blamm_stats *out)
+{
+    if (!ctx || !out) return BLAMM_ERR_ARG;
+    *out = ctx->stats;
+    return BLAMM_OK;
+}
+
+int blamm_guard_band(const blamm_ctx *ctx, float *out)
+{
+    if (!ctx || !out) return BLAMM_ERR_ARG;
+    blamm_ctx *c = const_cast<blamm_ctx *>(ctx);
+    if (c->mode == BLAMM_MODE_FP32) {
+        std::fill(out, out + c->ncols, 0.0f);
+        return BLAMM_OK;
+    }
+    int rc = ensure_plan(c);
+    if (rc) return rc;
+    std::copy(c->guard.begin(), c->guard.end(), out);
+    return BLAMM_OK;
+}
+
+int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0, int64_t npos, float *out)
+{
+    if (!ctx || !bases || !out || n <= 0 || p0 < 0 || npos <= 0 || p0 + npos > n) return BLAMM_ERR_ARG;
+    if (ctx->mode == BLAMM_MODE_FP32) return fail(ctx, BLAMM_ERR_STATE, "debug scores need a tcgen05 mode");
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_bases, bases, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    rc = launch_pack(ctx, ctx->d_bases, n);
+    if (rc) return rc;
+    int64_t runs0 = 0;
+    rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, 1);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_runs, &runs0, sizeof runs0, cudaMemcpyHostToDevice, ctx->stream));
+    float *d_dump = nullptr;
+    CK(cudaMalloc(&d_dump, sizeof(float) * (size_t)npos * ctx->ncols));
+    CK(cudaMemsetAsync(d_dump, 0, sizeof(float) * (size_t)npos * ctx->ncols, ctx->stream));
+    int launches = 0;
+    size_t hc = (size_t)ctx->hits_cap;
+    rc = ensure(ctx, &ctx->d_hits, &hc, 1);
+    if (rc) { cudaFree(d_dump); return rc; }
+    ctx->hits_cap = (int64_t)hc;
+    rc = run_tc(ctx, n, ctx->d_runs, 1, ctx->d_hits, 0, d_dump, p0, npos, &launches);
+    if (rc == BLAMM_OK) {
+        cudaError_t e = cudaMemcpyAsync(out, d_dump, sizeof(float) * (size_t)npos * ctx->ncols,
+                                        cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
+    }
+    cudaFree(d_dump);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+// host_capi.cpp -- the C ABI of include/blamm_host.h over MotifContainer.
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+
+#include "blamm_host.h"
+#include "histogram.h"
+#include "motif.h"
+
+struct blamm_bank {
+    blamm::MotifContainer motifs;
+};
+
+static thread_local std::string g_err;
+
+template <typename F>
+static int guarded(F &&f)
+{
+    try {
+        f();
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+extern "C" {
+
+const char *blamm_host_last_error(void) { return g_err.c_str(); }
+
+int blamm_bank_load(const char *motif_file, int load_permutations, int revcompl, blamm_bank **out)
+{
+    if (!motif_file || !out) return -1;
+    return guarded([&] {
+        auto *b = new blamm_bank();
+        try {
+            b->motifs.load(motif_file, load_permutations != 0);
+            if (revcompl) b->motifs.addReverseComplements();
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+    });
+}
+
+int blamm_bank_from_pfms(const uint64_t *pfm, const int32_t *lengths, int nmotifs, int revcompl, blamm_bank **out)
+{
+    if (!pfm || !lengths || nmotifs < 0 || !out) return -1;
+    return guarded([&] {
+        // write a Cluster-Buster stream and load it through the same parser/sort
+        std::string text;
+        size_t k = 0;
+        for (int i = 0; i < nmotifs; ++i) {
+            text += ">M" + std::to_string(i) + "\n";
+            for (int j = 0; j < lengths[i]; ++j, ++k) {
+                for (int b = 0; b < 4; ++b) {
+                    text += std::to_string(pfm[4 * k + b]);
+                    text += b < 3 ? '\t' : '\n';
+                }
+            }
+        }
+        char path[] = "/tmp/blamm_bank_XXXXXX";
+        const int fd = mkstemp(path);
+        if (fd < 0) throw std::runtime_error("cannot create a temporary file");
+        FILE *f = fdopen(fd, "w");
+        fwrite(text.data(), 1, text.size(), f);
+        fclose(f);
+        auto *b = new blamm_bank();
+        try {
+            b->motifs.load(path, true);
+            if (revcompl) b->motifs.addReverseComplements();
+        } catch (...) {
+            remove(path);
+            delete b;
+            throw;
+        }
+        remove(path);
+        *out = b;
+    });
+}
+
+void blamm_bank_free(blamm_bank *bank) { delete bank; }
+
+int blamm_bank_columns(const blamm_bank *bank) { return bank ? (int)bank->motifs.size() : -1; }
+
+int blamm_bank_max_len(const blamm_bank *bank) { return bank ? (int)bank->motifs.maxMotifLen() : -1; }
+
+int blamm_bank_generate(blamm_bank *bank, const uint64_t bg_counts[4], float pseudo)
+{
+    if (!bank || !bg_counts) return -1;
+    return guarded([&] {
+        bank->motifs.generateMatrix({bg_counts[0], bg_counts[1], bg_counts[2], bg_counts[3]}, pseudo);
+    });
+}
+
+int blamm_bank_matrix(const blamm_bank *bank, float *P, int32_t *lengths, int32_t *revcompl)
+{
+    if (!bank) return -1;
+    const auto &m = bank->motifs;
+    if (P) std::memcpy(P, m.matrix().data(), sizeof(float) * m.matrix().size());
+    for (size_t c = 0; c < m.size(); ++c) {
+        if (lengths) lengths[c] = (int32_t)m[c].size();
+        if (revcompl) revcompl[c] = m[c].isRevCompl() ? 1 : 0;
+    }
+    return 0;
+}
+
+int blamm_bank_min_max(const blamm_bank *bank, float *mn, float *mx)
+{
+    if (!bank || !mn || !mx) return -1;
+    for (size_t c = 0; c < bank->motifs.size(); ++c) {
+        mn[c] = bank->motifs[c].minScore();
+        mx[c] = bank->motifs[c].maxScore();
+    }
+    return 0;
+}
+
+int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4], int nbins, uint64_t max_length,
+                                 float pvalue, float *thr)
+{
+    if (!bank || !bg_prob || nbins < 2 || !thr) return -1;
+    return guarded([&] {
+        const std::array<float, 4> bg{bg_prob[0], bg_prob[1], bg_prob[2], bg_prob[3]};
+        std::map<std::string, float> cache;  // base name -> threshold of its forward motif
+        for (size_t c = 0; c < bank->motifs.size(); ++c) {
+            const blamm::Motif &m = bank->motifs[c];
+            if (m.isRevCompl()) continue;
+            const std::string key = m.baseName();
+            if (cache.count(key)) continue;
+            blamm::ScoreHistogram h(m.minScore(), m.maxScore(), (size_t)nbins);
+            blamm::theoreticalHistogram(m, bg, (size_t)max_length, h);
+            cache[key] = h.scoreCutoff(pvalue);
+        }
+        for (size_t c = 0; c < bank->motifs.size(); ++c) {
+            const std::string key = bank->motifs[c].baseName();
+            auto it = cache.find(key);
+            if (it == cache.end()) throw std::runtime_error("no forward motif for " + key);
+            thr[c] = it->second;
+        }
+    });
+}
+
+const char *blamm_bank_name(const blamm_bank *bank, int c)
+{
+    if (!bank || c < 0 || (size_t)c >= bank->motifs.size()) return nullptr;
+    return bank->motifs[(size_t)c].name().c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,401 @@
+// scan.cpp -- `blamm scan`: the drop-in PWMScan module driving libblamm_gpu.
+//
+// Same command line, thresholds, PWMthresholds.txt and occurrence format as
+// biointec/blamm's PWMScan (src/pwmscan.cpp:456-648, 81-102).  The BLAS /
+// cuBLAS block loop (scanThreadBLAS / scanThreadCUBLAS, :223-437) is replaced
+// by: a reader thread that streams FASTA into large overlapping chunks, one
+// worker per GPU that scans a chunk with one blamm_scan call (fused tcgen05
+// kernel), and a formatter that maps stream positions to (sequence, position)
+// and writes the lines.
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+#include "blamm_gpu.h"
+#include "histogram.h"
+#include "motif.h"
+#include "sequence.h"
+#include "species.h"
+
+namespace blamm {
+
+namespace {
+
+void scanUsage()
+{
+    std::cout << "Usage: blamm scan [options] motifs.input sequences.input\n"
+                 "Goal: find PWM matches in sequences\n\n"
+                 " [options]\n"
+                 "  -h\t--help\t\tdisplay help message\n"
+                 "  -s\t--simple\tscore lowercase bases too (the simple scan algorithm's scores)\n"
+                 "  -c\t--cuda\t\tenable the CUDA scan algorithm (always on)\n"
+                 "  -rc\t--revcompl\talso search the reverse strand for occurrences\n\n"
+                 " [options arg]\n"
+                 "  -at\t--absthreshold\tset the minimal absolute score for a motif occurrence\n"
+                 "  -rt\t--relthreshold\tset the minimal relative score [0..1] for a motif occurrence "
+                 "(default = 0.95)\n"
+                 "  -pt\t--pthreshold\tcompute the motif score threshold from p-value [0..1] (default = 1E-4)\n"
+                 "  -t\t--numthreads\tset the number of parallel threads [default = #cores]\n"
+                 "  -m\t--mode\t\tGPU arithmetic: bf16x2 (default), bf16 or fp32\n\n"
+                 " [file_options]\n"
+                 "  -H\t--histdir\tdirectory where the histogram file(s) are stored [default = .]\n"
+                 "  -o\t--output\tfilename for the motif occurrences [default = occurences.txt]\n\n"
+                 " Example:\n  blamm scan -o occurences.txt motifs.input sequences.input\n\n";
+}
+
+struct Options {
+    bool simple = false, revCompl = false;
+    bool absSet = false, relSet = false, pSet = false;
+    float absThreshold = 0.0f, relThreshold = 0.95f, pvalue = 0.0001f;
+    size_t numThreads = std::max(1u, std::thread::hardware_concurrency());
+    std::string histdir, output = "occurrences.txt";
+    int mode = BLAMM_MODE_BF16X2;
+};
+
+// One GPU context per device (the reference runs one host thread per device,
+// pwmscan.cpp:439-453).
+struct Device {
+    blamm_ctx *ctx = nullptr;
+    std::vector<blamm_hit> hits;
+};
+
+void check(blamm_ctx *ctx, int rc, const char *what)
+{
+    if (rc != BLAMM_OK)
+        throw std::runtime_error(std::string("GPU error in ") + what + ": " + blamm_last_error(ctx));
+}
+
+// scan one chunk on one device, growing the hit buffer on overflow
+void scanChunk(Device &dev, const StreamChunk &chunk)
+{
+    const std::vector<int64_t> runs = chunk.runStarts();
+    if (dev.hits.empty()) dev.hits.resize(1 << 20);
+    while (true) {
+        int64_t nh = 0;
+        const int rc = blamm_scan(dev.ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
+                                  (int64_t)runs.size(), dev.hits.data(), (int64_t)dev.hits.size(), &nh);
+        if (rc == BLAMM_ERR_OVERFLOW) {
+            dev.hits.resize((size_t)(nh + nh / 8 + 1024));
+            continue;
+        }
+        check(dev.ctx, rc, "blamm_scan");
+        dev.hits.resize((size_t)nh);  // hits beyond nh were never written
+        return;
+    }
+}
+
+// format "seq\tblamm\tmotif\tstart\tend\tscore\tstrand\t.\t." lines (pwmscan.cpp:88-95);
+// floats as the reference's default ostream (%g, 6 significant digits)
+void formatHits(const std::vector<blamm_hit> &hits, size_t lo, size_t hi, const StreamChunk &chunk,
+                const Species &species, const MotifContainer &motifs, std::string &out)
+{
+    char buf[64];
+    for (size_t i = lo; i < hi; ++i) {
+        const blamm_hit &h = hits[i];
+        const Marker m = chunk.locate(h.pos);
+        const Motif &mo = motifs[(size_t)h.col];
+        const std::string &seqName = (size_t)m.seqIdx < species.seqNames().size()
+                                         ? species.seqName((size_t)m.seqIdx)
+                                         : std::string();
+        out += seqName;
+        out += "\tblamm\t";
+        out += mo.name();
+        int k = snprintf(buf, sizeof buf, "\t%lld\t%lld\t%g\t%c\t.\t.\n", (long long)m.seqPos,
+                         (long long)(m.seqPos + (int64_t)mo.size()), (double)h.score,
+                         mo.isRevCompl() ? '-' : '+');
+        out.append(buf, (size_t)k);
+    }
+}
+
+}  // namespace
+
+// Histogram::generateEmpiricalHist / histThread (hist.cpp:95-160) on the GPU:
+// the first maxLength filtered bases of the species, FP32 scores of every
+// motif (forward strand) at every position whose window fits its run.
+void empiricalHistograms(const Species &species, MotifContainer &motifs, size_t maxLength,
+                         std::vector<ScoreHistogram> &hists)
+{
+    if (motifs.size() == 0) return;
+    blamm_ctx *ctx = nullptr;
+    if (blamm_ctx_create(0, &ctx) != BLAMM_OK) throw std::runtime_error("cannot create a GPU context");
+    std::unique_ptr<blamm_ctx, void (*)(blamm_ctx *)> guard(ctx, blamm_ctx_destroy);
+    std::vector<int32_t> lens(motifs.size());
+    std::vector<float> thr(motifs.size(), 0.0f), mn(motifs.size()), w(motifs.size());
+    for (size_t c = 0; c < motifs.size(); ++c) {
+        lens[c] = (int32_t)motifs[c].size();
+        mn[c] = hists[c].minScore();
+        w[c] = hists[c].width();
+    }
+    check(ctx, blamm_set_motifs(ctx, motifs.matrix().data(), (int)motifs.matrixRows(), (int)motifs.size(),
+                                lens.data(), thr.data()),
+          "blamm_set_motifs");
+    FastaStream fs(species.sequenceFilenames(), (int64_t)maxLength);
+    StreamChunk chunk;
+    const int64_t all = (int64_t)maxLength + 1;
+    if (!fs.nextChunk(chunk, all, 0)) return;
+    const size_t nbins = hists[0].numBins();
+    std::vector<uint64_t> counts(motifs.size() * nbins, 0);
+    const std::vector<int64_t> runs = chunk.runStarts();
+    check(ctx, blamm_score_histograms(ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
+                                      (int64_t)runs.size(), mn.data(), w.data(), (int)nbins, counts.data()),
+          "blamm_score_histograms");
+    for (size_t c = 0; c < motifs.size(); ++c)
+        for (size_t b = 0; b < nbins; ++b) hists[c].counts()[b] += counts[c * nbins + b];
+}
+
+int runScanModule(int argc, char **argv)
+{
+    if (argc < 4) {
+        scanUsage();
+        exit(EXIT_FAILURE);
+    }
+    Options o;
+    for (int i = 2; i < argc - 2; ++i) {
+        const std::string arg(argv[i]);
+        if (arg == "-h" || arg == "--help") {
+            scanUsage();
+            exit(EXIT_SUCCESS);
+        } else if (arg == "-rc" || arg == "--revcompl") {
+            o.revCompl = true;
+        } else if (arg == "-s" || arg == "--simple") {
+            o.simple = true;
+        } else if (arg == "-c" || arg == "--cuda") {
+        } else if ((arg == "-at" || arg == "--absthreshold") && i + 1 < argc - 2) {
+            o.absSet = true;
+            o.absThreshold = (float)std::atof(argv[++i]);
+        } else if ((arg == "-rt" || arg == "--relthreshold") && i + 1 < argc - 2) {
+            o.relSet = true;
+            o.relThreshold = (float)std::atof(argv[++i]);
+            if (o.relThreshold < 0.0 || o.relThreshold > 1.0)
+                throw std::runtime_error("The relative threshold should be in range [0..1].");
+        } else if ((arg == "-pt" || arg == "--pthreshold") && i + 1 < argc - 2) {
+            o.pSet = true;
+            o.pvalue = (float)std::atof(argv[++i]);
+            if (o.pvalue < 0.0 || o.pvalue > 1.0) throw std::runtime_error("The p-value should be in range [0..1].");
+        } else if ((arg == "-t" || arg == "--numthreads") && i + 1 < argc - 2) {
+            const int t = std::atoi(argv[++i]);
+            if (t < 1) throw std::runtime_error("Number of threads must be a non-zero positive number");
+            o.numThreads = (size_t)t;
+        } else if ((arg == "-H" || arg == "--histdir") && i + 1 < argc - 2) {
+            o.histdir = argv[++i];
+            if (o.histdir.back() != '/') o.histdir.push_back('/');
+        } else if ((arg == "-o" || arg == "--output") && i + 1 < argc - 2) {
+            o.output = argv[++i];
+        } else if ((arg == "-m" || arg == "--mode") && i + 1 < argc - 2) {
+            const std::string m(argv[++i]);
+            if (m == "fp32") o.mode = BLAMM_MODE_FP32;
+            else if (m == "bf16") o.mode = BLAMM_MODE_BF16;
+            else if (m == "bf16x2") o.mode = BLAMM_MODE_BF16X2;
+            else throw std::runtime_error("unknown mode " + m + " (bf16x2, bf16 or fp32)");
+        } else {
+            scanUsage();
+            exit(EXIT_FAILURE);
+        }
+    }
+    if (!(o.absSet || o.relSet || o.pSet)) o.relSet = true;
+    if (o.absSet && o.relSet) throw std::runtime_error("Specify either the absolute or relative threshold, not both.");
+    if (o.absSet && o.pSet) throw std::runtime_error("Specify either the absolute or p-value threshold, not both.");
+    if (o.relSet && o.pSet) throw std::runtime_error("Specify either the relative or p-value threshold, not both.");
+
+    std::cout << "Welcome to blamm -- PWM scan module" << std::endl;
+    Settings settings;
+    settings.print();
+    SpeciesContainer species;
+    species.load(std::string(argv[argc - 1]) + ".dict");
+    MotifContainer motifs;
+    motifs.load(argv[argc - 2], true);
+    std::cout << "Loaded " << motifs.size() << " motifs from disk\n";
+    std::cout << "Maximum motif size: " << motifs.maxMotifLen() << std::endl;
+    if (o.revCompl) {
+        motifs.addReverseComplements();
+        std::cout << "Scanning both forward and reverse strand of the input sequence(s)" << std::endl;
+    } else {
+        std::cout << "Scanning only the forward strand of the input sequence(s)" << std::endl;
+    }
+    motifs.generateMatrixTiles(settings.matrix_P_tile_min_zero_area, true);
+    if (o.absSet) std::cout << "Absolute motif score threshold set to: " << o.absThreshold << std::endl;
+    else if (o.relSet) std::cout << "Relative motif score threshold set to: " << o.relThreshold << std::endl;
+    else std::cout << "P-value motif score threshold set to: " << o.pvalue << std::endl;
+
+    int ndev = 0;
+    if (blamm_device_count(&ndev) != BLAMM_OK || ndev == 0) {
+        std::cerr << "CUDA error: no devices found. Aborting..." << std::endl;
+        return 1;
+    }
+    std::vector<Device> devs((size_t)ndev);
+    for (int d = 0; d < ndev; ++d) {
+        const int rc = blamm_ctx_create(d, &devs[(size_t)d].ctx);
+        if (rc != BLAMM_OK) throw std::runtime_error("cannot create a GPU context on device " + std::to_string(d));
+        check(devs[(size_t)d].ctx, blamm_set_mode(devs[(size_t)d].ctx, o.mode), "blamm_set_mode");
+        if (o.simple) check(devs[(size_t)d].ctx, blamm_set_softmask(devs[(size_t)d].ctx, 1), "blamm_set_softmask");
+    }
+    std::cout << "Using " << ndev << " GPU devices" << std::endl;
+
+    std::ofstream ofsCutoff("PWMthresholds.txt");
+    std::ofstream os(o.output.c_str(), std::ios::binary);
+    if (!os) throw std::runtime_error("Cannot write to file: " + o.output);
+    size_t totMatches = 0;
+
+    for (const auto &sp : species) {
+        std::cout << "Scanning species: " << sp.name() << std::endl;
+        motifs.generateMatrix(sp.nuclCounts(), settings.pseudocount);
+        for (auto &m : motifs) {
+            if (o.absSet) {
+                m.setThreshold(o.absThreshold);
+            } else if (o.relSet) {
+                const float mx = m.maxScore(), mn = m.minScore();
+                m.setThreshold(o.relThreshold * (mx - mn) + mn);
+            } else {
+                ScoreHistogram h;
+                h.loadHistogram(o.histdir, "hist_" + sp.name() + "_" + m.baseName());
+                m.setThreshold(h.scoreCutoff(o.pvalue));
+            }
+        }
+        for (auto &m : motifs) {
+            if (m.size() > 15) continue;
+            ofsCutoff << sp.name() << "\t" << m.name() << "\t" << m.minScore() << "\t" << m.threshold() << "\t"
+                      << m.maxScore() << std::endl;
+        }
+        if (motifs.size() == 0) continue;
+        std::vector<int32_t> lens(motifs.size());
+        std::vector<float> thr(motifs.size());
+        for (size_t c = 0; c < motifs.size(); ++c) {
+            lens[c] = (int32_t)motifs[c].size();
+            thr[c] = motifs[c].threshold();
+        }
+        for (auto &d : devs)
+            check(d.ctx, blamm_set_motifs(d.ctx, motifs.matrix().data(), (int)motifs.matrixRows(),
+                                          (int)motifs.size(), lens.data(), thr.data()),
+                  "blamm_set_motifs");
+
+        // reader -> per-device workers -> ordered writer
+        FastaStream fs(sp.sequenceFilenames(), (int64_t)sp.totalSeqLength());
+        const int64_t overlap = (int64_t)motifs.maxMotifLen() - 1;
+        const char *env = std::getenv("BLAMM_CHUNK_BASES");
+        const int64_t payload = env ? std::max<int64_t>(1, std::atoll(env)) : (int64_t)1 << 26;
+        std::mutex mu;
+        std::condition_variable cv;
+        std::deque<std::pair<size_t, std::shared_ptr<StreamChunk>>> todo;
+        std::map<size_t, std::string> done;
+        size_t nextRead = 0, nextWrite = 0;
+        bool readerDone = false;
+        std::exception_ptr failure;
+        std::thread reader([&] {
+            try {
+                while (true) {
+                    {
+                        std::unique_lock<std::mutex> lk(mu);
+                        cv.wait(lk, [&] { return todo.size() < devs.size() + 1 || failure; });
+                        if (failure) break;
+                    }
+                    auto chunk = std::make_shared<StreamChunk>();
+                    if (!fs.nextChunk(*chunk, payload, overlap)) break;
+                    std::lock_guard<std::mutex> lk(mu);
+                    todo.emplace_back(nextRead++, chunk);
+                    cv.notify_all();
+                }
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(mu);
+                failure = std::current_exception();
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            readerDone = true;
+            cv.notify_all();
+        });
+        auto worker = [&](Device &dev) {
+            try {
+                while (true) {
+                    std::pair<size_t, std::shared_ptr<StreamChunk>> job;
+                    {
+                        std::unique_lock<std::mutex> lk(mu);
+                        cv.wait(lk, [&] { return !todo.empty() || readerDone || failure; });
+                        if (failure || (todo.empty() && readerDone)) return;
+                        job = todo.front();
+                        todo.pop_front();
+                        cv.notify_all();
+                    }
+                    const StreamChunk &chunk = *job.second;
+                    scanChunk(dev, chunk);
+                    // keep the chunk's own positions (the overlap belongs to the next chunk)
+                    auto &h = dev.hits;
+                    h.erase(std::remove_if(h.begin(), h.end(),
+                                           [&](const blamm_hit &x) { return x.pos >= chunk.payload; }),
+                            h.end());
+                    std::sort(h.begin(), h.end(), [](const blamm_hit &a, const blamm_hit &b) {
+                        return a.pos != b.pos ? a.pos < b.pos : a.col < b.col;
+                    });
+                    // format in parallel slices
+                    const size_t nt = std::max<size_t>(1, std::min<size_t>(o.numThreads, h.size() / 20000 + 1));
+                    std::vector<std::string> parts(nt);
+                    std::vector<std::thread> th;
+                    for (size_t t = 0; t < nt; ++t)
+                        th.emplace_back([&, t] {
+                            formatHits(h, h.size() * t / nt, h.size() * (t + 1) / nt, chunk, sp, motifs, parts[t]);
+                        });
+                    for (auto &x : th) x.join();
+                    std::string text;
+                    for (auto &p : parts) text += p;
+                    std::unique_lock<std::mutex> lk(mu);
+                    totMatches += h.size();
+                    done.emplace(job.first, std::move(text));
+                    cv.notify_all();
+                }
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(mu);
+                failure = std::current_exception();
+                cv.notify_all();
+            }
+        };
+        std::vector<std::thread> workers;
+        for (auto &d : devs) workers.emplace_back(worker, std::ref(d));
+        // writer (this thread): chunks in stream order
+        while (true) {
+            std::string text;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] {
+                    return failure || done.count(nextWrite) || (readerDone && todo.empty() && nextWrite >= nextRead &&
+                                                                 done.empty());
+                });
+                if (failure) break;
+                auto it = done.find(nextWrite);
+                if (it == done.end()) {
+                    if (readerDone && todo.empty() && nextWrite >= nextRead) break;
+                    continue;
+                }
+                text = std::move(it->second);
+                done.erase(it);
+                ++nextWrite;
+            }
+            os << text;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (!failure && !readerDone) failure = std::make_exception_ptr(std::runtime_error("writer stopped"));
+            cv.notify_all();
+        }
+        reader.join();
+        for (auto &w : workers) w.join();
+        if (failure) std::rethrow_exception(failure);
+        std::cout << "Progress... 100%  " << std::endl;
+    }
+    os.close();
+    ofsCutoff.close();
+    for (auto &d : devs) blamm_ctx_destroy(d.ctx);
+    std::cout << "\nWrote " << totMatches << " matches to " << o.output << ".\n";
+    return 0;
+}
+
+}  // namespace blamm

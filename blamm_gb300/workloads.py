@@ -1,0 +1,212 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+The reference ships no benchmark data; these generators stand in for it:
+  config 1  32 motifs (L 6-20), 2 x 500 kbp iid (A=T=0.3, C=G=0.2)
+  config 2  512 motifs (L 5-30), 24 sequences log-uniform 1-20 Mbp, ~100 Mbp total
+            iid (A=T=0.29, C=G=0.21)
+  config 3  2000 motifs (L 5-30), 1 Gbp, 2nd-order Markov background (GC ~ 0.41),
+            1 % of bases in N runs of length log-uniform 100-10k
+  config 4  10,000 sequences, log-normal lengths (median 2 kbp, sigma 1.0,
+            clipped 200-50k), GC 0.5, 800 motifs (L 6-25)
+Motif columns are Multinomial(100, Dirichlet(0.5 * 1_4)) counts.  Random
+streams: numpy default_rng with separate children for motifs, lengths, bases.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+ACGT = np.frombuffer(b"ACGT", dtype=np.uint8)
+
+
+def rngs(seed: int) -> tuple[np.random.Generator, np.random.Generator, np.random.Generator]:
+    ss = np.random.SeedSequence(seed)
+    m, l, b = ss.spawn(3)
+    return np.random.default_rng(m), np.random.default_rng(l), np.random.default_rng(b)
+
+
+def random_pfms(rng: np.random.Generator, nmotifs: int, lmin: int, lmax: int, total: int = 100,
+                alpha: float = 0.5) -> list[tuple[str, np.ndarray]]:
+    out = []
+    for i in range(nmotifs):
+        L = int(rng.integers(lmin, lmax + 1))
+        probs = rng.dirichlet([alpha] * 4, size=L)
+        counts = np.stack([rng.multinomial(total, p) for p in probs]).astype(np.uint64)
+        out.append((f"MOTIF{i:05d}", counts))
+    return out
+
+
+def iid_bases(rng: np.random.Generator, n: int, probs) -> np.ndarray:
+    idx = rng.choice(4, size=n, p=np.asarray(probs, dtype=np.float64))
+    return ACGT[idx]
+
+
+def markov2_bases(rng: np.random.Generator, n: int, gc: float = 0.41) -> np.ndarray:
+    """2nd-order Markov chain: seeded 16 x 4 transition table, rows tilted to the GC target."""
+    table = rng.dirichlet([2.0] * 4, size=16)
+    target = np.array([(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])
+    table = table * target
+    table /= table.sum(axis=1, keepdims=True)
+    cdf = np.cumsum(table, axis=1)
+    u = rng.random(n)
+    out = np.empty(n, dtype=np.uint8)
+    # vectorised in chunks: the state depends on the previous two symbols only
+    state = 0
+    chunk = 1 << 16
+    codes = np.empty(n, dtype=np.uint8)
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        for i in range(s, e):
+            c = int(np.searchsorted(cdf[state], u[i], side="right"))
+            c = min(c, 3)
+            codes[i] = c
+            state = ((state << 2) | c) & 15
+    out[:] = ACGT[codes]
+    return out
+
+
+def insert_n_runs(rng: np.random.Generator, seq: np.ndarray, frac: float, lmin: int = 100,
+                  lmax: int = 10000) -> np.ndarray:
+    """Overwrite ~frac of the bases with N runs of log-uniform length."""
+    n = len(seq)
+    seq = seq.copy()
+    budget = int(frac * n)
+    while budget > 0:
+        L = int(np.exp(rng.uniform(np.log(lmin), np.log(lmax))))
+        L = min(L, budget)
+        s = int(rng.integers(0, max(1, n - L)))
+        seq[s:s + L] = ord("N")
+        budget -= L
+    return seq
+
+
+@dataclass
+class Workload:
+    """FASTA-level description: named sequences (raw bytes, may contain N) + motif PFMs."""
+    name: str
+    sequences: list[tuple[str, np.ndarray]]
+    motifs: list[tuple[str, np.ndarray]]
+    pvalue: float = 1e-4
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def total_bases(self) -> int:
+        return int(sum(len(s) for _, s in self.sequences))
+
+
+def config1(seed: int = 0, seq_len: int = 500_000) -> Workload:
+    rm, rl, rb = rngs(seed)
+    motifs = random_pfms(rm, 32, 6, 20)
+    seqs = [(f"seq{i}", iid_bases(rb, seq_len, [0.3, 0.2, 0.2, 0.3])) for i in range(2)]
+    return Workload("config1", seqs, motifs, 1e-4)
+
+
+def config2(seed: int = 0, total: int = 100_000_000, nseq: int = 24) -> Workload:
+    rm, rl, rb = rngs(seed)
+    motifs = random_pfms(rm, 512, 5, 30)
+    raw = np.exp(rl.uniform(np.log(1e6), np.log(2e7), size=nseq))
+    lens = np.maximum(1, np.round(raw / raw.sum() * total)).astype(np.int64)
+    seqs = [(f"chr{i + 1}", iid_bases(rb, int(L), [0.29, 0.21, 0.21, 0.29])) for i, L in enumerate(lens)]
+    return Workload("config2", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+
+
+def config3(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Workload:
+    rm, rl, rb = rngs(seed)
+    motifs = random_pfms(rm, 2000, 5, 30)
+    raw = np.exp(rl.uniform(np.log(1e6), np.log(2e7), size=nseq))
+    lens = np.maximum(1, np.round(raw / raw.sum() * total)).astype(np.int64)
+    seqs = []
+    for i, L in enumerate(lens):
+        # iid with GC 0.41 stands in for the Markov chain at full size (python loop too slow);
+        # markov2_bases() is used at reduced sizes
+        s = iid_bases(rb, int(L), [0.295, 0.205, 0.205, 0.295])
+        seqs.append((f"chr{i + 1}", insert_n_runs(rb, s, 0.01)))
+    return Workload("config3", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+
+
+def config4(seed: int = 0, nseq: int = 10_000) -> Workload:
+    rm, rl, rb = rngs(seed)
+    motifs = random_pfms(rm, 800, 6, 25)
+    lens = np.clip(np.round(np.exp(rl.normal(np.log(2000), 1.0, size=nseq))), 200, 50_000).astype(np.int64)
+    seqs = [(f"prom{i}", iid_bases(rb, int(L), [0.25, 0.25, 0.25, 0.25])) for i, L in enumerate(lens)]
+    return Workload("config4", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+
+
+# ---------------------------------------------------------------- writers
+def write_fasta(path: str, sequences: list[tuple[str, np.ndarray]], width: int = 60) -> None:
+    with open(path, "wb") as f:
+        for name, seq in sequences:
+            f.write(b">" + name.encode() + b"\n")
+            b = seq.tobytes()
+            for i in range(0, len(b), width):
+                f.write(b[i:i + width] + b"\n")
+
+
+def write_jaspar(path: str, motifs: list[tuple[str, np.ndarray]]) -> None:
+    with open(path, "w") as f:
+        for name, pfm in motifs:
+            f.write(f">{name}\t{name}\n")
+            for k, ch in enumerate("ACGT"):
+                f.write(ch + "  [ " + " ".join(f"{int(v):5d}" for v in pfm[:, k]) + " ]\n")
+
+
+def write_cb(path: str, motifs: list[tuple[str, np.ndarray]]) -> None:
+    with open(path, "w") as f:
+        for name, pfm in motifs:
+            f.write(f">{name}\n")
+            for row in pfm:
+                f.write("\t".join(str(int(v)) for v in row) + "\n")
+
+
+def write_settings(path: str, w: int = 250, h: int = 1000, tile_area: int = 4096,
+                   pseudo: float = 0.25, flush: int = 100000) -> None:
+    with open(path, "w") as f:
+        f.write(f"MATRIX_S_W\t{w}\nMATRIX_S_H\t{h}\nMATRIX_P_TILE_MIN_ZERO_AREA\t{tile_area}\n"
+                f"PSEUDOCOUNT\t{pseudo}\nFLUSHOUTPUT\t{flush}\n")
+
+
+def write_case(directory: str, groups: dict[str, list[tuple[str, list[tuple[str, np.ndarray]]]]],
+               motifs: list[tuple[str, np.ndarray]], jaspar: bool = True) -> tuple[str, str]:
+    """groups: {group: [(fasta_file_name, sequences), ...]} -> (motif_file, manifest)."""
+    os.makedirs(directory, exist_ok=True)
+    lines = []
+    for g, files in groups.items():
+        for fname, seqs in files:
+            write_fasta(os.path.join(directory, fname), seqs)
+            lines.append(f"{g}\t{fname}\n")
+    manifest = os.path.join(directory, "sequences.mf")
+    with open(manifest, "w") as f:
+        f.writelines(lines)
+    mfile = os.path.join(directory, "motifs.jaspar" if jaspar else "motifs.cb")
+    (write_jaspar if jaspar else write_cb)(mfile, motifs)
+    return mfile, manifest
+
+
+# ---------------------------------------------------------------- streams
+def filtered_stream(sequences: list[tuple[str, np.ndarray]]):
+    """FASTA content -> (bases, run_start, run_seq, run_seqpos): maximal runs of ACGTacgt.
+
+    Same stream the host library builds from FASTA files (one line per
+    sequence, so line breaks never split a run)."""
+    valid = np.zeros(256, dtype=bool)
+    valid[np.frombuffer(b"ACGTacgt", dtype=np.uint8)] = True
+    parts, starts, rseq, rpos = [], [], [], []
+    n = 0
+    for si, (_, seq) in enumerate(sequences):
+        v = valid[seq]
+        if not v.any():
+            continue
+        d = np.diff(np.concatenate([[0], v.view(np.int8), [0]]))
+        b = np.flatnonzero(d == 1)
+        e = np.flatnonzero(d == -1)
+        for s0, e0 in zip(b, e):
+            starts.append(n)
+            rseq.append(si)
+            rpos.append(int(s0))
+            parts.append(seq[s0:e0])
+            n += int(e0 - s0)
+    bases = np.concatenate(parts) if parts else np.zeros(0, dtype=np.uint8)
+    return (bases, np.asarray(starts, dtype=np.int64), np.asarray(rseq, dtype=np.int64),
+            np.asarray(rpos, dtype=np.int64))

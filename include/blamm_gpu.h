@@ -1,0 +1,152 @@
+/*
+ * blamm_gpu.h -- C ABI of the GB300 (sm_103a) PWM scan library, libblamm_gpu.so.
+ *
+ * The library replaces the compute seam of biointec/blamm's scan module:
+ *   - Matrix::sgemm_batch / sgemm_batch_cuda (src/matrix.h:292-323), the
+ *     batched S x P products, one per column offset,
+ *   - kernel_wrapper / filterScore (src/kernel.cu:21-45), the threshold filter
+ *     and hit compaction, and
+ *   - PWMScan::extractOccurrences / extractOccurrences2 (src/pwmscan.cpp:104-163),
+ *     the threshold and run-length checks,
+ * with one fused call that takes the filtered base stream of a species and
+ * returns its occurrences.  The one-hot S matrix and the score matrix R never
+ * exist in memory.  Scores are bit-identical to the reference's FP32 sgemm
+ * sums (sequential in motif position), and so is the hit set.
+ *
+ * Conventions: plain pointers and sizes, no C++ types; every call returns a
+ * status (0 = ok, negative = error; blamm_last_error() has the message).  A
+ * context belongs to one host thread at a time (the reference runs one host
+ * thread per device, src/pwmscan.cpp:439-453); contexts are independent.
+ */
+#ifndef BLAMM_GPU_H
+#define BLAMM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BLAMM_OK 0
+#define BLAMM_ERR_ARG (-1)         /* invalid argument */
+#define BLAMM_ERR_CUDA (-2)        /* CUDA runtime error */
+#define BLAMM_ERR_OVERFLOW (-3)    /* hit buffer too small; *n_hits holds the total */
+#define BLAMM_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+#define BLAMM_ERR_NOMEM (-5)       /* device allocation failed */
+#define BLAMM_ERR_UNSUPPORTED (-6) /* e.g. no sm_100-class GPU, motif too long */
+#define BLAMM_ERR_STATE (-7)       /* call order (e.g. scan before set_motifs) */
+
+/* arithmetic of the contraction (the emitted scores are FP32-exact in all modes) */
+#define BLAMM_MODE_FP32 0   /* plain SIMT FP32 sums: the straightforward GPU form */
+#define BLAMM_MODE_BF16 1   /* tcgen05, P as one BF16 term, wide guard band */
+#define BLAMM_MODE_BF16X2 2 /* tcgen05, P split hi+lo BF16 (two MMAs), narrow guard band */
+
+typedef struct blamm_ctx blamm_ctx;
+
+/* One occurrence (the fields of MotifOccurrence, src/motif.h:557-641, before
+ * the stream position is mapped to (sequence, position)). */
+typedef struct {
+    int64_t pos;  /* stream position of the first motif base */
+    int32_t col;  /* column of P (motif index in the MotifContainer) */
+    float score;  /* FP32 score, equal to the reference's R(i, j) */
+} blamm_hit;
+
+/* Statistics of the last scan on a context. */
+typedef struct {
+    int64_t positions;   /* stream positions scanned */
+    int64_t columns;     /* motif columns scanned */
+    int64_t candidates;  /* positions x columns that passed the guard band */
+    int64_t hits;        /* occurrences found */
+    int32_t tiles;       /* motif tiles (tcgen05 N tiles) */
+    int32_t launches;    /* kernels launched by the last scan */
+    float kernel_ms;     /* device time of the scan kernels (CUDA events) */
+    float total_ms;      /* device time of the whole call incl. copies */
+} blamm_stats;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int blamm_version(void);
+
+/* Create a context on a CUDA device (own stream, own device buffers).
+ * Replaces the per-thread set-up of PWMScan::scanThreadCUBLAS
+ * (src/pwmscan.cpp:297-360): cudaSetDevice, cublasCreate, cudaMalloc. */
+int blamm_ctx_create(int device, blamm_ctx **out);
+void blamm_ctx_destroy(blamm_ctx *ctx);
+const char *blamm_last_error(const blamm_ctx *ctx);
+
+/* Select the arithmetic (BLAMM_MODE_*).  Default BLAMM_MODE_BF16X2. */
+int blamm_set_mode(blamm_ctx *ctx, int mode);
+
+/* Upload the motif bank.  P is MotifContainer's matrix (src/motif.cpp:542-564):
+ * column-major FP32, p_rows x ncols, p_rows = 4 * (longest motif), column c
+ * holding motif c's PWM as P(4j+b, c) (b = A,C,G,T) and zeros below 4*len[c].
+ * thr[c] is the score threshold of column c (Motif::getThreshold; set at
+ * src/pwmscan.cpp:599-616).  Replaces the d_P / d_threshold uploads of
+ * src/pwmscan.cpp:317-342 and the P tiling of MotifContainer::generateMatrixTiles
+ * (src/motif.cpp:482-540), which the library re-plans for the tensor cores. */
+int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols,
+                     const int32_t *col_len, const float *thr);
+
+/* Replace the thresholds only (per species / per p-value), keeping the bank. */
+int blamm_set_thresholds(blamm_ctx *ctx, const float *thr);
+
+/* Scan a filtered base stream held in host memory.
+ * bases: n characters from {A,C,G,T,a,c,g,t} -- the content of the reference's
+ *   SeqBlock stream (src/sequence.cpp:181-250).  Lowercase bases are scanned
+ *   positions but add nothing to a score, as in the one-hot S of
+ *   src/sequence.cpp:306-337.
+ * run_start: nruns ascending stream positions, run_start[0] == 0, one per
+ *   maximal contiguous run (the SeqBlock markers, src/sequence.cpp:81-88).
+ *   A window that crosses into the next run is not a hit (src/pwmscan.cpp:122-126).
+ * Writes up to hit_cap hits (unordered) and their number to *n_hits.
+ * Returns BLAMM_ERR_OVERFLOW, with *n_hits = the total, when hit_cap is too small. */
+int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+               int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits);
+
+/* The same on device-resident data (device pointers, the context's stream):
+ * nothing is copied between host and device except the hit count. */
+int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n,
+                      const int64_t *d_run_start, int64_t nruns, blamm_hit *d_hits,
+                      int64_t hit_cap, int64_t *n_hits);
+
+/* Drop-in for the reference's kernel_wrapper (src/kernel.cu:36-45): for the
+ * column-major m x n matrix d_R, append every entry R(i,j) >= d_threshold[j]
+ * to d_occScore / d_occIdx (index j*m+i) at atomically reserved slots of
+ * *d_nOcc.  Device pointers; runs on the context's stream and synchronises. */
+int blamm_filter_score(blamm_ctx *ctx, float *d_R, int m, int n, const float *d_threshold,
+                       int *d_occIdx, float *d_occScore, int *d_nOcc);
+
+/* Number of CUDA devices (0 when there is no driver or device). */
+int blamm_device_count(int *n);
+
+/* Soft-masked (lowercase) bases: 0 (default) = they add nothing to a score,
+ * as in the reference's BLAS/cuBLAS scan (src/sequence.cpp:312-318);
+ * 1 = they score like uppercase, as in its simple scan (`scan -s`,
+ * Motif::getScore, src/motif.cpp:225-239). */
+int blamm_set_softmask(blamm_ctx *ctx, int lowercase_scores);
+
+/* Empirical score histograms (the `hist -e` module, src/hist.cpp:70-140):
+ * for every position whose window fits inside its run, add the FP32 score of
+ * each column c to bin int((score - min_score[c]) / width[c]) clamped to
+ * [0, nbins-1] (ScoreHistogram::addObservation, src/motif.h:96-102).
+ * counts is ncols x nbins, row-major, and is accumulated into. */
+int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                           int64_t nruns, const float *min_score, const float *width, int nbins,
+                           uint64_t *counts);
+
+/* Statistics of the last scan. */
+int blamm_last_stats(const blamm_ctx *ctx, blamm_stats *out);
+
+/* Test and measurement hooks.
+ * blamm_debug_scores: for positions [p0, p0+npos) of a host stream, the raw
+ * tensor-core score of every column (row-major npos x ncols) -- the value the
+ * guard band is applied to -- in the current tcgen05 mode. */
+int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0, int64_t npos,
+                       float *out);
+/* The guard band of each column in the current mode (ncols floats). */
+int blamm_guard_band(const blamm_ctx *ctx, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,63 @@
+/*
+ * blamm_host.h -- C ABI of the host library libblamm_host.so: the motif-bank
+ * side of biointec/blamm's scan path (MotifContainer, Motif, ScoreHistogram;
+ * src/motif.h, src/motif.cpp), for callers that drive libblamm_gpu.so
+ * without the `blamm` command line (language bindings, benchmarks, services).
+ *
+ * A bank is a MotifContainer: motifs sorted by length, optionally with their
+ * reverse complements interleaved ([m0, rc(m0), m1, rc(m1), ...]); column c
+ * of its matrix P is motif c.  Every call returns 0 on success, negative on
+ * error (blamm_host_last_error() has the message, per thread).
+ */
+#ifndef BLAMM_HOST_H
+#define BLAMM_HOST_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct blamm_bank blamm_bank;
+
+const char *blamm_host_last_error(void);
+
+/* MotifContainer::load (src/motif.cpp:323-338) + addReverseComplements (:439-449).
+ * motif_file: JASPAR when it ends in ".jaspar", Cluster-Buster otherwise. */
+int blamm_bank_load(const char *motif_file, int load_permutations, int revcompl, blamm_bank **out);
+
+/* A bank from in-memory PFMs: pfm holds the motifs' L x 4 (A,C,G,T) counts
+ * back to back, lengths[i] their lengths; names are "M<i>".  Sorted by length
+ * like a loaded file. */
+int blamm_bank_from_pfms(const uint64_t *pfm, const int32_t *lengths, int nmotifs, int revcompl,
+                         blamm_bank **out);
+void blamm_bank_free(blamm_bank *bank);
+
+int blamm_bank_columns(const blamm_bank *bank);  /* motifs in the container */
+int blamm_bank_max_len(const blamm_bank *bank);
+
+/* MotifContainer::generateMatrix (src/motif.cpp:542-564): PWMs for the
+ * background counts (A,C,G,T) and pseudocount, and the matrix P. */
+int blamm_bank_generate(blamm_bank *bank, const uint64_t bg_counts[4], float pseudo);
+
+/* P as column-major floats (columns x 4*max_len), lengths, strands (1 = rc). */
+int blamm_bank_matrix(const blamm_bank *bank, float *P, int32_t *lengths, int32_t *revcompl);
+
+/* Motif::getMinScore / getMaxScore per column (src/motif.cpp:241-265). */
+int blamm_bank_min_max(const blamm_bank *bank, float *min_score, float *max_score);
+
+/* p-value thresholds from theoretical histograms: per column, the histogram of
+ * `hist` (src/hist.cpp:162-175; nbins bins, max_length observations, iid
+ * background probabilities bg_prob) of the forward motif of the same name,
+ * inverted at pvalue (ScoreHistogram::getScoreCutoff, src/motif.cpp:47-69).
+ * Histograms are kept in memory (no text round trip of the .dat files). */
+int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4], int nbins,
+                                 uint64_t max_length, float pvalue, float *thr);
+
+/* Name of column c (valid until the bank is freed). */
+const char *blamm_bank_name(const blamm_bank *bank, int c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
