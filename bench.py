@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 PWM scan: bp*motif/s on the 512-motif x 100 Mbp workload.
+
+One step = one scan of the whole synthetic stream (both strands, p = 1e-4
+thresholds from theoretical histograms) through libblamm_gpu's C ABI:
+  value : device-resident stream and hit buffer (blamm_scan_device), CUDA events
+          on the library's stream around every step, L2 flushed between steps
+  e2e   : host buffers (blamm_scan): H2D of the stream and run table, the scan,
+          D2H of the hits, wall clock per step
+The headline mode is the BF16 hi+lo split on tcgen05; the single-term BF16 and
+the plain FP32 GPU forms run on the same stream and must give the same hits.
+`--impl reference` times the reference's own CPU algorithm (the oracle's port of
+its BLAS loop; the reference binary cannot be built on the GPU host) instead.
+
+Prints one JSON line (rank 0).  Multi-GPU (torchrun): each rank scans its own
+contiguous share of the sequences, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bp·motif/s on 1 GB300, BF16-split vs FP32 plain (same hits); serve p50/p99 ms"
+UNIT = "bp·motif/s"
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--bases", type=int, default=100_000_000, help="total bases of the workload")
+    ap.add_argument("--cpu-sample", type=int, default=8_000_000, help="bases in a CPU-baseline sample")
+    ap.add_argument("--no-modes", action="store_true", help="skip the bf16 / fp32 comparison runs")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ workload
+def build_workload(seed: int, total: int):
+    from blamm_gb300 import workloads
+    from blamm_gb300._native import MotifBank
+    wl = workloads.config2(seed, total=total)
+    bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
+    counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
+    bank = MotifBank.from_pfms([p for _, p in wl.motifs], revcompl=True)
+    bank.generate(counts, 0.25)
+    P, lens, _ = bank.matrix()
+    tot = np.float32(counts.sum()) + np.float32(4.0) * np.float32(0.25)
+    bgp = ((counts.astype(np.float32) + np.float32(0.25)) / tot).astype(np.float32)
+    thr = bank.pvalue_thresholds(bgp, wl.pvalue)
+    return wl, bases, runs, rseq, P, lens, thr
+
+
+def shard(bases, runs, rseq, rank, world):
+    """Contiguous share of the sequences for one rank (no data exchange)."""
+    if world == 1:
+        return bases, runs
+    n = len(bases)
+    seq_ids = np.unique(rseq)
+    starts = np.array([runs[np.flatnonzero(rseq == s)[0]] for s in seq_ids] + [n])
+    targets = np.linspace(0, n, world + 1)
+    cut = [0] + [int(starts[np.argmin(np.abs(starts - t))]) for t in targets[1:-1]] + [n]
+    lo, hi = cut[rank], cut[rank + 1]
+    sel = (runs >= lo) & (runs < hi)
+    return bases[lo:hi], (runs[sel] - lo).astype(np.int64)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops, burst)"
+    return 1900.0, "fallback 1.9 PFLOP/s"
+
+
+def profile_traffic(positions: int):
+    """DRAM bytes of one scan-kernel launch, scaled from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "scan_tc_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    return int(d["dram_bytes"] * positions / d["positions"])
+
+
+def hit_digest(h: np.ndarray) -> tuple[int, int]:
+    """Order-independent digest of a hit set (count, checksum of pos/col/score bits)."""
+    key = (h["pos"].astype(np.uint64) * np.uint64(1_000_003) + h["col"].astype(np.uint64)) ^ (
+        h["score"].view(np.uint32).astype(np.uint64) << np.uint64(20))
+    return int(len(h)), int(np.bitwise_xor.reduce(key * np.uint64(0x9E3779B97F4A7C15)) if len(h) else 0)
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_sample_scan(bases, runs, P, lens, thr, sample: int):
+    """The reference's BLAS loop (oracle port) on the first `sample` bases, all cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    b = bases[:sample]
+    r = runs[runs < len(b)]
+    tiles = oracle.matrix_tiles(lens, 4096)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    h = oracle.scan_blas(b, r, P, lens, thr, tiles, 1000, 250, cores)
+    dt = time.perf_counter() - t0
+    return len(b) * P.shape[0] / dt, cores, dt, len(h)
+
+
+def run_reference(a, rank, world):
+    """--impl reference: the reference's CPU scan (oracle port of its BLAS loop) per step."""
+    if rank != 0:
+        return
+    wl, bases, runs, rseq, P, lens, thr = build_workload(a.seed, a.bases)
+    sample = min(a.cpu_sample, len(bases))
+    for _ in range(a.warmup):
+        cpu_sample_scan(bases, runs, P, lens, thr, sample)
+    vals, times = [], []
+    cores = 1
+    for _ in range(a.steps):
+        v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, sample)
+        vals.append(v)
+        times.append(dt)
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic",
+        "config": {"workload": f"config2: 512 motifs (1024 columns, L 5-30, both strands) x "
+                               f"{len(bases)} bp, p=1e-4; each step a {sample} bp sample"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"first {sample} bp of the stream x 1024 columns, "
+                                   "the reference's BLAS block loop (h=1000, w=250) on OpenBLAS"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU side
+def run_ours(a, rank, world, local):
+    import torch
+    from blamm_gb300 import GpuScanner, HIT_DTYPE
+    from blamm_gb300._native import gpu_lib
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    wl, bases_all, runs_all, rseq, P, lens, thr = build_workload(a.seed, a.bases)
+    bases, runs = shard(bases_all, runs_all, rseq, rank, world)
+    n, ncols = len(bases), P.shape[0]
+    units = n * ncols
+    flops_per_bp = float(8 * lens.astype(np.int64).sum())
+
+    sc = GpuScanner(local, "bf16x2")
+    sc.set_motifs(P, lens, thr)
+    ext = torch.cuda.ExternalStream(sc.stream())
+    d_bases = torch.from_numpy(bases).to(f"cuda:{local}")
+    d_runs = torch.from_numpy(runs).to(f"cuda:{local}")
+    cap = max(1 << 20, units // 2000)
+    d_hits = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def device_steps(k: int, record: bool):
+        ms, scan_ms, launches, nh = [], [], 0, 0
+        for i in range(k):
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            nh = sc.scan_device(d_bases.data_ptr(), n, d_runs.data_ptr(), len(runs), d_hits.data_ptr(), cap)
+            e1.record(ext)
+            e1.synchronize()
+            st = sc.stats()
+            if record:
+                ms.append(e0.elapsed_time(e1))
+                scan_ms.append(st["scan_ms"])
+                launches += st["launches"]
+        return ms, scan_ms, launches, nh
+
+    def hits_on_device(nh: int) -> np.ndarray:
+        return d_hits[: nh * HIT_DTYPE.itemsize].cpu().numpy().view(HIT_DTYPE)
+
+    # ---- headline mode: BF16 hi+lo
+    device_steps(max(a.warmup, 3), False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ms, scan_ms, launches, nh = device_steps(a.steps, True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    step_ms = float(np.sum(ms)) / a.steps
+    if dist:
+        t = torch.tensor([step_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+        u = torch.tensor([float(units)], device=f"cuda:{local}")
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        total_units = float(u.item())
+    else:
+        total_units = float(units)
+    value = total_units / (step_ms / 1e3)
+    st = sc.stats()
+    ref_digest = hit_digest(hits_on_device(nh))
+
+    # ---- the same step end to end through host buffers (pinned)
+    lib = gpu_lib()
+    hb = torch.from_numpy(bases).pin_memory()
+    hr = torch.from_numpy(runs).pin_memory()
+    hh = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    nhc = C.c_int64(0)
+
+    def e2e_step():
+        rc = lib.blamm_scan(sc.h, C.c_void_p(hb.data_ptr()), n, C.c_void_p(hr.data_ptr()), len(runs),
+                            C.c_void_p(hh.data_ptr()), cap, C.byref(nhc))
+        if rc != 0:
+            raise RuntimeError(lib.blamm_last_error(sc.h).decode())
+    for _ in range(max(a.warmup, 3)):
+        e2e_step()
+    e2e_t = []
+    for _ in range(a.steps):
+        t1 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_digest = hit_digest(hh[: nhc.value * HIT_DTYPE.itemsize].numpy().view(HIT_DTYPE))
+    e2e_value = total_units / float(np.mean(e2e_t)) if world == 1 else units / float(np.mean(e2e_t)) * world
+
+    # ---- other modes on the same stream (same hits required)
+    modes = {}
+    if not a.no_modes:
+        for mode in ("bf16", "fp32"):
+            sc.set_mode(mode)
+            device_steps(1, False)
+            mms, msc, _, mnh = device_steps(max(1, min(3, a.steps)), True)
+            mst = sc.stats()
+            modes[mode] = {"value": units / (float(np.mean(mms)) / 1e3), "ms_per_step": float(np.mean(mms)),
+                           "scan_kernel_ms": float(np.mean(msc)), "hits": int(mnh),
+                           "candidates": int(mst["candidates"]),
+                           "same_hits_as_bf16x2": hit_digest(hits_on_device(mnh)) == ref_digest}
+        sc.set_mode("bf16x2")
+
+    # ---- roofline of the dominant kernel (tcgen05 scan)
+    peak, peak_src = peaks()
+    kern_ms = float(np.mean(scan_ms))
+    achieved = n * flops_per_bp / (kern_ms / 1e3) / 1e12
+    traffic = profile_traffic(n)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x2 (hi+lo fixed-point split, fp32 accumulate) + fp32 rescoring",
+        "data": "synthetic (seeded numpy, config2 shapes)",
+        "config": {"workload": "config2: 512 motifs (1024 columns, L 5-30, both strands, Dirichlet(0.5) "
+                               "columns of 100 counts) x 24 iid sequences (A=T=0.29) log-uniform 1-20 Mbp, "
+                               f"{n} bp per rank, p=1e-4 theoretical-histogram thresholds",
+                   "bases_per_rank": n, "columns": ncols, "l2": "flushed (256 MiB write between steps)",
+                   "parallelism": f"{world} rank(s), contiguous sequence shards, no collective"},
+        "hits": int(nh), "candidates": int(st["candidates"]), "tiles": int(st["tiles"]),
+        "scan_kernel_ms": kern_ms, "rescore_kernel_ms": float(st["rescore_ms"]),
+        "wall_s_timed_region": wall,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n + 8 * len(runs)),
+                "d2h_bytes_per_step": int(16 * nhc.value + 8), "ms_per_step": 1e3 * float(np.mean(e2e_t)),
+                "same_hits": e2e_digest == ref_digest},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": f"algorithmic flops = 8 * sum(L) = {flops_per_bp:.0f} per bp per launch over "
+                             f"{n} bp; the hi+lo split issues 2 MMAs per flop (ceiling 0.5); peak {peak_src}"},
+        "modes": modes,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1:
+        v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"first {min(a.cpu_sample, n)} bp x {ncols} columns in {dt:.1f} s: the "
+                                          "reference's BLAS block loop (h=1000, w=250, OpenBLAS sgemm per tile "
+                                          "per offset, one BLAS thread per worker)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sc.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = args_parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    run_ours(a, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -35,7 +35,8 @@ class BlammError(RuntimeError):
 class Stats(C.Structure):
     _fields_ = [("positions", C.c_int64), ("columns", C.c_int64), ("candidates", C.c_int64),
                 ("hits", C.c_int64), ("tiles", C.c_int32), ("launches", C.c_int32),
-                ("kernel_ms", C.c_float), ("total_ms", C.c_float)]
+                ("kernel_ms", C.c_float), ("total_ms", C.c_float), ("scan_ms", C.c_float),
+                ("rescore_ms", C.c_float)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -69,9 +70,14 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_last_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.blamm_debug_scores.argtypes = [vp, vp, i64, i64, i64, f32p]
     lib.blamm_guard_band.argtypes = [vp, f32p]
+    lib.blamm_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+    lib.blamm_device_count.argtypes = [C.POINTER(C.c_int)]
+    lib.blamm_set_softmask.argtypes = [vp, C.c_int]
+    lib.blamm_score_histograms.argtypes = [vp, vp, i64, vp, i64, vp, vp, C.c_int, vp]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
-                 "blamm_debug_scores", "blamm_guard_band"):
+                 "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
+                 "blamm_set_softmask", "blamm_score_histograms"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -156,6 +162,25 @@ class GpuScanner:
         self._check(rc)
         return nh.value
 
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        p = C.c_void_p()
+        self._check(self.lib.blamm_ctx_stream(self.h, C.byref(p)))
+        return p.value or 0
+
+    def set_softmask(self, lowercase_scores: bool) -> None:
+        self._check(self.lib.blamm_set_softmask(self.h, int(bool(lowercase_scores))))
+
+    def score_histograms(self, bases, run_start, min_score, width, nbins: int) -> np.ndarray:
+        b = np.ascontiguousarray(bases, dtype=np.uint8)
+        runs = np.ascontiguousarray(run_start, dtype=np.int64)
+        mn = np.ascontiguousarray(min_score, dtype=np.float32)
+        w = np.ascontiguousarray(width, dtype=np.float32)
+        out = np.zeros((self.ncols, nbins), dtype=np.uint64)
+        self._check(self.lib.blamm_score_histograms(self.h, _ptr(b), len(b), _ptr(runs), len(runs), _ptr(mn),
+                                                    _ptr(w), nbins, _ptr(out)))
+        return out
+
     def stats(self) -> dict:
         s = Stats()
         self._check(self.lib.blamm_last_stats(self.h, C.byref(s)))
@@ -179,3 +204,170 @@ class GpuScanner:
         self._check(self.lib.blamm_filter_score(self.h, C.c_void_p(d_R), m, n, C.c_void_p(d_thr),
                                                 C.c_void_p(d_idx), C.c_void_p(d_score),
                                                 C.c_void_p(d_nocc)))
+
+
+# ---------------------------------------------------------------- host library
+_host = None
+
+
+def host_lib() -> C.CDLL:
+    """Load libblamm_host.so (motif banks, PWMs, histograms); raises if it is missing."""
+    global _host
+    if _host is not None:
+        return _host
+    if not os.path.exists(HOST_LIB_PATH):
+        raise ImportError(f"{HOST_LIB_PATH} is missing: run `python -m blamm_gb300.build` first")
+    gpu_lib()  # dependency, loaded from the same directory
+    lib = C.CDLL(HOST_LIB_PATH)
+    vp = C.c_void_p
+    lib.blamm_host_last_error.restype = C.c_char_p
+    lib.blamm_bank_load.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(vp)]
+    lib.blamm_bank_from_pfms.argtypes = [vp, vp, C.c_int, C.c_int, C.POINTER(vp)]
+    lib.blamm_bank_free.argtypes = [vp]
+    lib.blamm_bank_free.restype = None
+    lib.blamm_bank_columns.argtypes = [vp]
+    lib.blamm_bank_max_len.argtypes = [vp]
+    lib.blamm_bank_generate.argtypes = [vp, vp, C.c_float]
+    lib.blamm_bank_matrix.argtypes = [vp, vp, vp, vp]
+    lib.blamm_bank_min_max.argtypes = [vp, vp, vp]
+    lib.blamm_bank_pvalue_thresholds.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, vp]
+    lib.blamm_bank_name.argtypes = [vp, C.c_int]
+    lib.blamm_bank_name.restype = C.c_char_p
+    for name in ("blamm_bank_load", "blamm_bank_from_pfms", "blamm_bank_columns", "blamm_bank_max_len",
+                 "blamm_bank_generate", "blamm_bank_matrix", "blamm_bank_min_max",
+                 "blamm_bank_pvalue_thresholds"):
+        getattr(lib, name).restype = C.c_int
+    _host = lib
+    return lib
+
+
+class MotifBank:
+    """A MotifContainer of the host library (sorted by length, optional rc columns)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self.lib = host_lib()
+        self.h = handle
+
+    @classmethod
+    def load(cls, motif_file: str, permutations: bool = True, revcompl: bool = True) -> "MotifBank":
+        lib = host_lib()
+        h = C.c_void_p()
+        if lib.blamm_bank_load(motif_file.encode(), int(permutations), int(revcompl), C.byref(h)) != 0:
+            raise BlammError(-1, lib.blamm_host_last_error().decode())
+        return cls(h)
+
+    @classmethod
+    def from_pfms(cls, pfms: list[np.ndarray], revcompl: bool = True) -> "MotifBank":
+        lib = host_lib()
+        lens = np.array([p.shape[0] for p in pfms], dtype=np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.uint64).reshape(-1, 4) for p in pfms]))
+        h = C.c_void_p()
+        if lib.blamm_bank_from_pfms(_ptr(flat), _ptr(lens), len(pfms), int(revcompl), C.byref(h)) != 0:
+            raise BlammError(-1, lib.blamm_host_last_error().decode())
+        return cls(h)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.blamm_bank_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def columns(self) -> int:
+        return self.lib.blamm_bank_columns(self.h)
+
+    @property
+    def max_len(self) -> int:
+        return self.lib.blamm_bank_max_len(self.h)
+
+    def generate(self, bg_counts, pseudo: float = 0.25) -> None:
+        bg = np.ascontiguousarray(bg_counts, dtype=np.uint64)
+        if self.lib.blamm_bank_generate(self.h, _ptr(bg), pseudo) != 0:
+            raise BlammError(-1, self.lib.blamm_host_last_error().decode())
+
+    def matrix(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(P as (columns, 4*max_len) float32, lengths, rc flags) after generate()."""
+        n, L = self.columns, self.max_len
+        P = np.zeros((n, 4 * L), dtype=np.float32)
+        lens = np.zeros(n, dtype=np.int32)
+        rc = np.zeros(n, dtype=np.int32)
+        self.lib.blamm_bank_matrix(self.h, _ptr(P), _ptr(lens), _ptr(rc))
+        return P, lens, rc
+
+    def min_max(self) -> tuple[np.ndarray, np.ndarray]:
+        mn = np.zeros(self.columns, dtype=np.float32)
+        mx = np.zeros(self.columns, dtype=np.float32)
+        self.lib.blamm_bank_min_max(self.h, _ptr(mn), _ptr(mx))
+        return mn, mx
+
+    def pvalue_thresholds(self, bg_prob, pvalue: float, nbins: int = 250,
+                          max_length: int = 10_000_000) -> np.ndarray:
+        bg = np.ascontiguousarray(bg_prob, dtype=np.float32)
+        thr = np.zeros(self.columns, dtype=np.float32)
+        if self.lib.blamm_bank_pvalue_thresholds(self.h, _ptr(bg), nbins, max_length, pvalue, _ptr(thr)) != 0:
+            raise BlammError(-1, self.lib.blamm_host_last_error().decode())
+        return thr
+
+    def name(self, c: int) -> str:
+        return self.lib.blamm_bank_name(self.h, c).decode()
+
+
+class FastaReader:
+    """Chunks of the filtered base stream of FASTA files (host library)."""
+
+    def __init__(self, files: list[str], max_filt: int = -1):
+        self.lib = host_lib()
+        L = self.lib
+        vp, i64 = C.c_void_p, C.c_int64
+        L.blamm_fasta_open.argtypes = [C.POINTER(C.c_char_p), C.c_int, i64, C.POINTER(vp)]
+        L.blamm_fasta_open.restype = C.c_int
+        L.blamm_fasta_next.argtypes = [vp, i64, i64, C.POINTER(vp), C.POINTER(i64), C.POINTER(i64),
+                                       C.POINTER(i64), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                                       C.POINTER(i64)]
+        L.blamm_fasta_next.restype = C.c_int
+        L.blamm_fasta_num_sequences.argtypes = [vp]
+        L.blamm_fasta_num_sequences.restype = i64
+        L.blamm_fasta_sequence_name.argtypes = [vp, i64]
+        L.blamm_fasta_sequence_name.restype = C.c_char_p
+        L.blamm_fasta_close.argtypes = [vp]
+        L.blamm_fasta_close.restype = None
+        arr = (C.c_char_p * len(files))(*[f.encode() for f in files])
+        self.h = C.c_void_p()
+        if L.blamm_fasta_open(arr, len(files), max_filt, C.byref(self.h)) != 0:
+            raise BlammError(-1, L.blamm_host_last_error().decode())
+
+    def next_chunk(self, payload: int, overlap: int):
+        """(offset, payload, bases uint8, markers (k, 3) int64) or None at the end."""
+        b, mp, ms, mq = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        size, pay, off, nm = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        rc = self.lib.blamm_fasta_next(self.h, payload, overlap, C.byref(b), C.byref(size), C.byref(pay),
+                                       C.byref(off), C.byref(mp), C.byref(ms), C.byref(mq), C.byref(nm))
+        if rc < 0:
+            raise BlammError(rc, self.lib.blamm_host_last_error().decode())
+        if rc == 0:
+            return None
+        bases = np.ctypeslib.as_array(C.cast(b, C.POINTER(C.c_uint8)), (size.value,)).copy() if size.value else \
+            np.zeros(0, np.uint8)
+        k = nm.value
+        cols = [np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int64)), (k,)).copy() for p in (mp, ms, mq)]
+        return off.value, pay.value, bases, np.stack(cols, axis=1)
+
+    def sequence_names(self) -> list[str]:
+        n = self.lib.blamm_fasta_num_sequences(self.h)
+        return [self.lib.blamm_fasta_sequence_name(self.h, i).decode() for i in range(n)]
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.blamm_fasta_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

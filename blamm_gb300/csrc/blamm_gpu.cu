@@ -27,9 +27,10 @@ struct blamm_ctx {
     int sm_count = 0;
     int max_smem = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::string err;
     int mode = BLAMM_MODE_BF16X2;
+    bool plain_timed = false, rescore_timed = false;
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
 
@@ -513,8 +514,10 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         p.dump_ncols = ctx->ncols;
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
         if (njobs > 0) {
+            CK(cudaEventRecord(ctx->ev[4], ctx->stream));
             scan_tc_kernel<<<grid, kTcThreads, smem, ctx->stream>>>(p);
             CK(cudaGetLastError());
+            CK(cudaEventRecord(ctx->ev[5], ctx->stream));
             ++*launches;
         }
         unsigned long long ncand = 0;
@@ -523,6 +526,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         if (status) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
+        if (njobs > 0) cudaEventElapsedTime(&ctx->stats.scan_ms, ctx->ev[4], ctx->ev[5]);
         ctx->stats.candidates = (int64_t)ncand;
         if ((int64_t)ncand <= ctx->cand_cap) break;
         // grow and re-run
@@ -555,8 +559,11 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     if (nc > 0) {
         const int threads = 256;
         const int64_t blocks = std::min<int64_t>((nc + threads - 1) / threads, (int64_t)ctx->sm_count * 16);
+        CK(cudaEventRecord(ctx->ev[6], ctx->stream));
         rescore_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(r);
         CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[7], ctx->stream));
+        ctx->rescore_timed = true;
         ++*launches;
     }
     return BLAMM_OK;
@@ -590,8 +597,11 @@ static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t n
     const int by = (ctx->ncols + cpb - 1) / cpb;
     if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
     if (bx > 0) {
+        CK(cudaEventRecord(ctx->ev[4], ctx->stream));
         scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
         CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[5], ctx->stream));
+        ctx->plain_timed = true;
         ++*launches;
     }
     return BLAMM_OK;
@@ -603,6 +613,7 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     int launches = 0;
     ctx->stats = blamm_stats{};
+    ctx->plain_timed = ctx->rescore_timed = false;
     ctx->stats.positions = n;
     ctx->stats.columns = ctx->ncols;
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
@@ -619,6 +630,8 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
     ctx->stats.kernel_ms = ms;
+    if (ctx->plain_timed) cudaEventElapsedTime(&ctx->stats.scan_ms, ctx->ev[4], ctx->ev[5]);
+    if (ctx->rescore_timed) cudaEventElapsedTime(&ctx->stats.rescore_ms, ctx->ev[6], ctx->ev[7]);
     ctx->stats.hits = (int64_t)nh;
     ctx->stats.tiles = (int32_t)(ctx->mode == BLAMM_MODE_FP32 ? 0 : ctx->tiles.size());
     ctx->stats.launches = launches;
@@ -791,6 +804,13 @@ int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const i
     cleanup();
     if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
     for (size_t i = 0; i < nc * (size_t)nbins; ++i) counts[i] += host[i];
+    return BLAMM_OK;
+}
+
+int blamm_ctx_stream(const blamm_ctx *ctx, void **stream)
+{
+    if (!ctx || !stream) return BLAMM_ERR_ARG;
+    *stream = (void *)ctx->stream;
     return BLAMM_OK;
 }
 

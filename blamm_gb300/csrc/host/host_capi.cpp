@@ -1,15 +1,25 @@
 // host_capi.cpp -- the C ABI of include/blamm_host.h over MotifContainer.
 #include <cstring>
+#include <limits>
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "blamm_host.h"
 #include "histogram.h"
 #include "motif.h"
+#include "sequence.h"
 
 struct blamm_bank {
     blamm::MotifContainer motifs;
+};
+
+struct blamm_fasta {
+    blamm::FastaStream stream;
+    blamm::StreamChunk chunk;
+    std::vector<int64_t> pos, seq, seqpos;
+    explicit blamm_fasta(std::vector<std::string> files, int64_t maxFilt) : stream(std::move(files), maxFilt) {}
 };
 
 static thread_local std::string g_err;
@@ -148,5 +158,53 @@ const char *blamm_bank_name(const blamm_bank *bank, int c)
     if (!bank || c < 0 || (size_t)c >= bank->motifs.size()) return nullptr;
     return bank->motifs[(size_t)c].name().c_str();
 }
+
+int blamm_fasta_open(const char *const *files, int nfiles, int64_t max_filt, blamm_fasta **out)
+{
+    if (!files || nfiles < 0 || !out) return -1;
+    return guarded([&] {
+        std::vector<std::string> v(files, files + nfiles);
+        *out = new blamm_fasta(v, max_filt < 0 ? std::numeric_limits<int64_t>::max() : max_filt);
+    });
+}
+
+int blamm_fasta_next(blamm_fasta *f, int64_t payload, int64_t overlap, const char **bases, int64_t *size,
+                     int64_t *chunk_payload, int64_t *offset, const int64_t **marker_pos,
+                     const int64_t **marker_seq, const int64_t **marker_seqpos, int64_t *nmarkers)
+{
+    if (!f || payload <= 0 || overlap < 0) return -1;
+    int got = 0;
+    const int rc = guarded([&] {
+        got = f->stream.nextChunk(f->chunk, payload, overlap) ? 1 : 0;
+        if (!got) return;
+        f->pos.clear();
+        f->seq.clear();
+        f->seqpos.clear();
+        for (const auto &m : f->chunk.markers) {
+            f->pos.push_back(m.streamPos);
+            f->seq.push_back(m.seqIdx);
+            f->seqpos.push_back(m.seqPos);
+        }
+        if (bases) *bases = f->chunk.bases.data();
+        if (size) *size = (int64_t)f->chunk.bases.size();
+        if (chunk_payload) *chunk_payload = f->chunk.payload;
+        if (offset) *offset = f->chunk.offset;
+        if (marker_pos) *marker_pos = f->pos.data();
+        if (marker_seq) *marker_seq = f->seq.data();
+        if (marker_seqpos) *marker_seqpos = f->seqpos.data();
+        if (nmarkers) *nmarkers = (int64_t)f->pos.size();
+    });
+    return rc ? rc : got;
+}
+
+int64_t blamm_fasta_num_sequences(const blamm_fasta *f) { return f ? (int64_t)f->stream.seqNames().size() : -1; }
+
+const char *blamm_fasta_sequence_name(const blamm_fasta *f, int64_t i)
+{
+    if (!f || i < 0 || (size_t)i >= f->stream.seqNames().size()) return nullptr;
+    return f->stream.seqNames()[(size_t)i].c_str();
+}
+
+void blamm_fasta_close(blamm_fasta *f) { delete f; }
 
 }  // extern "C"

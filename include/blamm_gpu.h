@@ -60,8 +60,10 @@ typedef struct {
     int64_t hits;        /* occurrences found */
     int32_t tiles;       /* motif tiles (tcgen05 N tiles) */
     int32_t launches;    /* kernels launched by the last scan */
-    float kernel_ms;     /* device time of the scan kernels (CUDA events) */
+    float kernel_ms;     /* device time of all kernels of the call (CUDA events) */
     float total_ms;      /* device time of the whole call incl. copies */
+    float scan_ms;       /* device time of the scan kernel alone (tcgen05 or plain FP32) */
+    float rescore_ms;    /* device time of the rescoring kernel (tcgen05 modes) */
 } blamm_stats;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -133,6 +135,10 @@ int blamm_set_softmask(blamm_ctx *ctx, int lowercase_scores);
 int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
                            int64_t nruns, const float *min_score, const float *width, int nbins,
                            uint64_t *counts);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events around the library's. */
+int blamm_ctx_stream(const blamm_ctx *ctx, void **stream);
 
 /* Statistics of the last scan. */
 int blamm_last_stats(const blamm_ctx *ctx, blamm_stats *out);

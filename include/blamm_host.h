@@ -57,6 +57,24 @@ int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4],
 /* Name of column c (valid until the bank is freed). */
 const char *blamm_bank_name(const blamm_bank *bank, int c);
 
+/* FASTA streaming (FastaBatch, src/sequence.cpp:123-293): the files' runs of
+ * A/C/G/T/a/c/g/t concatenated into one stream, cut into chunks of `payload`
+ * positions plus `overlap` bases that reappear at the start of the next chunk.
+ * max_filt truncates the stream (FastaBatch's maximum filtered length; -1 =
+ * no limit).  Each chunk comes with its markers: chunk position, sequence index
+ * and position inside the sequence of every run start (the first marker is at
+ * chunk position 0).  Chunk pointers stay valid until the next call. */
+typedef struct blamm_fasta blamm_fasta;
+int blamm_fasta_open(const char *const *files, int nfiles, int64_t max_filt, blamm_fasta **out);
+/* returns 1 and fills the outputs when a chunk was read, 0 at the end, <0 on error */
+int blamm_fasta_next(blamm_fasta *f, int64_t payload, int64_t overlap, const char **bases, int64_t *size,
+                     int64_t *chunk_payload, int64_t *offset, const int64_t **marker_pos,
+                     const int64_t **marker_seq, const int64_t **marker_seqpos, int64_t *nmarkers);
+/* sequences named so far (all of them once the stream is exhausted) */
+int64_t blamm_fasta_num_sequences(const blamm_fasta *f);
+const char *blamm_fasta_sequence_name(const blamm_fasta *f, int64_t i);
+void blamm_fasta_close(blamm_fasta *f);
+
 #ifdef __cplusplus
 }
 #endif

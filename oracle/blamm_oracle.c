@@ -489,11 +489,16 @@ static int64_t collect(scan_job *jobs, int nt, orc_hit *hits, int64_t cap)
     return tot;
 }
 
-static unsigned char *make_codes(const char *bases, int64_t n)
+static unsigned char *make_codes(const char *bases, int64_t n, int lower_scores)
 {
     unsigned char *code = (unsigned char *)malloc((size_t)n + 1);
     if (!code) return NULL;
-    for (int64_t i = 0; i < n; i++) code[i] = (unsigned char)base_code(bases[i]);
+    for (int64_t i = 0; i < n; i++) {
+        char c = bases[i];
+        /* Motif::getScore / char2idx (motif.cpp:138-149, 225-239) is case-insensitive */
+        if (lower_scores && c >= 'a' && c <= 'z') c = (char)(c - 32);
+        code[i] = (unsigned char)base_code(c);
+    }
     code[n] = 4;
     return code;
 }
@@ -503,10 +508,19 @@ int64_t orc_scan(const char *bases, int64_t n, const int64_t *run_start,
                  const int32_t *col_len, const float *thr, int nthreads,
                  orc_hit *hits, int64_t cap)
 {
+    return orc_scan_ex(bases, n, run_start, nruns, P, p_rows, ncols, col_len, thr,
+                       nthreads, 0, hits, cap);
+}
+
+int64_t orc_scan_ex(const char *bases, int64_t n, const int64_t *run_start,
+                    int64_t nruns, const float *P, int p_rows, int ncols,
+                    const int32_t *col_len, const float *thr, int nthreads,
+                    int lower_scores, orc_hit *hits, int64_t cap)
+{
     if (n < 0 || ncols < 0 || (n > 0 && nruns <= 0)) return -1;
     if (nthreads < 1) nthreads = 1;
     if (n == 0 || ncols == 0) return 0;
-    unsigned char *code = make_codes(bases, n);
+    unsigned char *code = make_codes(bases, n, lower_scores);
     if (!code) return -1;
     scan_job *jobs = (scan_job *)calloc((size_t)nthreads, sizeof(scan_job));
     pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
@@ -632,7 +646,7 @@ int64_t orc_scan_blas(const char *bases, int64_t n, const int64_t *run_start,
     if (n == 0 || ncols == 0) return 0;
     int maxlen = 0;
     for (int c = 0; c < ncols; c++) if (col_len[c] > maxlen) maxlen = col_len[c];
-    unsigned char *code = make_codes(bases, n);
+    unsigned char *code = make_codes(bases, n, 0);
     if (!code) return -1;
     int64_t payload = (int64_t)h * w;
     int64_t nblocks = (n + payload - 1) / payload;

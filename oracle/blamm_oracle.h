@@ -91,6 +91,14 @@ int64_t orc_scan(const char *bases, int64_t n, const int64_t *run_start,
                  const int32_t *col_len, const float *thr, int nthreads,
                  orc_hit *hits, int64_t cap);
 
+/* orc_scan with the simple scan's case handling (PWMScan::scanThreadNaive,
+ * pwmscan.cpp:165-206): lower_scores = 1 scores lowercase bases like uppercase
+ * (Motif::getScore, motif.cpp:225-239). */
+int64_t orc_scan_ex(const char *bases, int64_t n, const int64_t *run_start,
+                    int64_t nruns, const float *P, int p_rows, int ncols,
+                    const int32_t *col_len, const float *thr, int nthreads,
+                    int lower_scores, orc_hit *hits, int64_t cap);
+
 /* Same hit set, computed the reference's way: per block of h*w payload bases
  * (+ overlap), a one-hot S matrix, one BLAS sgemm per P tile per column offset,
  * then a threshold scan of R (pwmscan.cpp:223-278, matrix.h:292-306,

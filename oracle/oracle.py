@@ -31,6 +31,8 @@ def lib() -> C.CDLL:
         vp, i64 = C.c_void_p, C.c_int64
         L.orc_scan.argtypes = [vp, i64, vp, i64, vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, i64]
         L.orc_scan.restype = i64
+        L.orc_scan_ex.argtypes = [vp, i64, vp, i64, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, i64]
+        L.orc_scan_ex.restype = i64
         L.orc_scan_blas.argtypes = [vp, i64, vp, i64, vp, C.c_int, C.c_int, vp, vp, vp, C.c_int,
                                     C.c_int, C.c_int, C.c_int, vp, i64]
         L.orc_scan_blas.restype = i64
@@ -109,21 +111,21 @@ def matrix_tiles(lens, min_zero_area: int) -> np.ndarray:
 
 
 def scan(bases: np.ndarray, run_start: np.ndarray, P: np.ndarray, col_len, thr,
-         nthreads: int = 8) -> np.ndarray:
-    """Sequential-FP32 scan (the reference's hit set). P: (ncols, p_rows)."""
+         nthreads: int = 8, lower_scores: bool = False) -> np.ndarray:
+    """Sequential-FP32 scan (the reference's hit set). P: (ncols, p_rows).
+    lower_scores: lowercase bases score like uppercase (the simple scan, `scan -s`)."""
     b = np.ascontiguousarray(bases, dtype=np.uint8)
     runs = np.ascontiguousarray(run_start, dtype=np.int64)
     P = np.ascontiguousarray(P, dtype=np.float32)
     ln = np.ascontiguousarray(col_len, dtype=np.int32)
     th = np.ascontiguousarray(thr, dtype=np.float32)
     ncols, rows = P.shape
-    n = lib().orc_scan(_p(b), len(b), _p(runs), len(runs), _p(P), rows, ncols, _p(ln), _p(th),
-                       nthreads, None, 0)
+    args = (_p(b), len(b), _p(runs), len(runs), _p(P), rows, ncols, _p(ln), _p(th), nthreads, int(lower_scores))
+    n = lib().orc_scan_ex(*args, None, 0)
     if n < 0:
         raise RuntimeError("oracle scan failed")
     out = np.zeros(n, dtype=HIT_DTYPE)
-    lib().orc_scan(_p(b), len(b), _p(runs), len(runs), _p(P), rows, ncols, _p(ln), _p(th), nthreads,
-                   _p(out), n)
+    lib().orc_scan_ex(*args, _p(out), n)
     return out
 
 

@@ -540,13 +540,14 @@ static float hist_cutoff(const char *histdir, const char *spname, const char *mo
 static int run_scan(int argc, char **argv)
 {
     if (argc < 4) die("Usage: blamm scan [options] motifs.input sequences.input");
-    int rc = 0, nthreads = 8, abs_set = 0, rel_set = 0, p_set = 0;
+    int rc = 0, nthreads = 8, abs_set = 0, rel_set = 0, p_set = 0, simple = 0;
     float abs_t = 0.0f, rel_t = 0.95f, pval = 0.0001f;
     char histdir[4096] = "", outfn[4096] = "occurrences.txt";
     for (int i = 2; i < argc - 2; i++) {
         const char *a = argv[i];
         if (!strcmp(a, "-rc") || !strcmp(a, "--revcompl")) rc = 1;
-        else if (!strcmp(a, "-s") || !strcmp(a, "--simple") || !strcmp(a, "-c") || !strcmp(a, "--cuda")) {}
+        else if (!strcmp(a, "-s") || !strcmp(a, "--simple")) simple = 1;
+        else if (!strcmp(a, "-c") || !strcmp(a, "--cuda")) {}
         else if ((!strcmp(a, "-at") || !strcmp(a, "--absthreshold")) && i + 1 < argc - 2) { abs_set = 1; abs_t = (float)atof(argv[++i]); }
         else if ((!strcmp(a, "-rt") || !strcmp(a, "--relthreshold")) && i + 1 < argc - 2) {
             rel_set = 1; rel_t = (float)atof(argv[++i]);
@@ -611,12 +612,12 @@ static int run_scan(int argc, char **argv)
         if (orc_stream_read((const char *const *)sp[s].files, sp[s].nfiles, (int64_t)sp[s].tot,
                             &str, err, sizeof err))
             die(err);
-        int64_t nh = orc_scan(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len,
-                              thr, nthreads, NULL, 0);
+        int64_t nh = orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len,
+                                 thr, nthreads, simple, NULL, 0);
         if (nh < 0) die("oracle scan failed");
         orc_hit *hits = (orc_hit *)malloc(sizeof(orc_hit) * (size_t)(nh ? nh : 1));
-        orc_scan(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len, thr, nthreads,
-                 hits, nh);
+        orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len, thr, nthreads,
+                    simple, hits, nh);
         int64_t r = 0;
         for (int64_t h = 0; h < nh; h++) {
             int64_t p = hits[h].pos;

@@ -1,0 +1,146 @@
+"""Host side (C++ libblamm_host.so + the `blamm` CLI without a GPU) against the oracle
+and the reference's golden files."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+import oracle
+from blamm_gb300 import workloads
+from blamm_gb300._native import CLI_PATH, FastaReader, MotifBank
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("case", gc.CASES)
+def test_cli_dict_and_hist_match_reference(tmp_path, case):
+    spec = gc.load(case)
+    d = gc.stage(case, str(tmp_path))
+    gc.run(CLI_PATH, d, spec, skip=[lambda c: c[0] == "scan", lambda c: c[0] == "hist" and "-e" in c])
+    gc.compare(d, case, spec, what=("dict", "hist"))
+
+
+def _pfms(seed, n, lmin, lmax):
+    return [p for _, p in workloads.random_pfms(np.random.default_rng(seed), n, lmin, lmax)]
+
+
+def test_bank_matrix_equals_oracle_pwms():
+    pf = _pfms(31, 40, 4, 30)
+    bank = MotifBank.from_pfms(pf, revcompl=True)
+    bg = [12345, 6789, 7000, 13000]
+    bank.generate(bg, 0.25)
+    P, lens, rc = bank.matrix()
+    order = sorted(range(len(pf)), key=lambda i: pf[i].shape[0])
+    # the container is sorted by length (std::sort; equal lengths may permute), so match by content
+    cols = []
+    for i in order:
+        cols.append((oracle.pfm2pwm(pf[i], bg, 0.25, False), 0))
+        cols.append((oracle.pfm2pwm(oracle.revcompl_pfm(pf[i]), bg, 0.25, True), 1))
+    got = {(P[c, :4 * lens[c]].tobytes(), int(rc[c])) for c in range(P.shape[0])}
+    want = {(w.tobytes(), r) for w, r in cols}
+    assert got == want
+    assert np.all(np.diff(lens) >= 0)
+    assert np.all(rc[1::2] == 1) and np.all(rc[0::2] == 0)
+    mn, mx = bank.min_max()
+    for c in range(P.shape[0]):
+        omn, omx = oracle.min_max_score(P[c, :4 * lens[c]].reshape(-1, 4))
+        assert (mn[c], mx[c]) == (np.float32(omn), np.float32(omx))
+
+
+def test_bank_pvalue_thresholds_equal_oracle():
+    pf = _pfms(32, 12, 5, 25)
+    bank = MotifBank.from_pfms(pf, revcompl=True)
+    counts = [2900, 2100, 2100, 2900]
+    bank.generate(counts, 0.25)
+    P, lens, rc = bank.matrix()
+    bgp = oracle.nucl_prob(counts, 0.25)
+    thr = bank.pvalue_thresholds(bgp, 1e-4, 250, 10_000_000)
+    for c in range(0, P.shape[0], 2):  # forward columns; rc columns share the threshold
+        pwm = P[c, :4 * lens[c]].reshape(-1, 4)
+        mn, mx = oracle.min_max_score(pwm)
+        width = np.float32(np.float32(mx) - np.float32(mn)) / np.float32(250)
+        h = oracle.theoretical_hist(pwm, bgp, 250, 10_000_000)
+        want = oracle.score_cutoff(h, mn, float(width), mx, 1e-4)
+        assert np.float32(thr[c]) == np.float32(want) and thr[c + 1] == thr[c]
+
+
+def _oracle_stream(files, max_filt=-1):
+    """orc_stream_read through ctypes: (bases, run_start, run_seq, run_seqpos, names)."""
+    L = oracle.lib()
+
+    class S(C.Structure):
+        _fields_ = [("bases", C.c_void_p), ("n", C.c_int64), ("run_start", C.c_void_p),
+                    ("run_seq", C.c_void_p), ("run_seqpos", C.c_void_p), ("nruns", C.c_int64),
+                    ("names", C.c_void_p), ("nseq", C.c_int64), ("tot_seq_len", C.c_int64)]
+    L.orc_stream_read.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.c_int64, C.POINTER(S), C.c_char_p, C.c_int]
+    L.orc_stream_free.argtypes = [C.POINTER(S)]
+    s = S()
+    err = C.create_string_buffer(512)
+    arr = (C.c_char_p * len(files))(*[f.encode() for f in files])
+    assert L.orc_stream_read(arr, len(files), max_filt, C.byref(s), err, 512) == 0, err.value
+    def a64(p, k):
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int64)), (k,)).copy() if k else np.zeros(0, np.int64)
+    bases = np.ctypeslib.as_array(C.cast(s.bases, C.POINTER(C.c_uint8)), (s.n,)).copy() if s.n else np.zeros(0, np.uint8)
+    out = (bases, a64(s.run_start, s.nruns), a64(s.run_seq, s.nruns), a64(s.run_seqpos, s.nruns))
+    L.orc_stream_free(C.byref(s))
+    return out
+
+
+@pytest.mark.parametrize("payload,overlap", [(10_000_000, 29), (997, 29), (4096, 0), (50, 23)])
+@pytest.mark.parametrize("max_filt", [-1, 30_001])
+def test_fasta_chunks_equal_oracle_stream(payload, overlap, max_filt):
+    files = [os.path.join(gc.GOLDEN, "mixed", "seqs", f) for f in ("a_file.fa", "b_file.fa")]
+    bases, rs, rq, rp = _oracle_stream(files, max_filt)
+    rd = FastaReader(files, max_filt)
+    pos = 0
+    while True:
+        ch = rd.next_chunk(payload, overlap)
+        if ch is None:
+            break
+        off, pay, b, mk = ch
+        assert off == pos
+        assert np.array_equal(b, bases[off:off + len(b)])
+        assert len(b) == min(payload + overlap, len(bases) - off) and pay == min(payload, len(b))
+        # every chunk position maps to the same (sequence, position) as in the oracle's stream
+        r = np.searchsorted(rs, off + mk[:, 0], side="right") - 1
+        assert np.array_equal(rq[r], mk[:, 1])
+        assert np.array_equal(rp[r] + (off + mk[:, 0] - rs[r]), mk[:, 2])
+        # markers inside the chunk are exactly the oracle's run starts there
+        inside = rs[(rs > off) & (rs < off + len(b))] - off
+        assert np.array_equal(mk[1:, 0], inside) and mk[0, 0] == 0
+        pos += pay
+    assert pos == len(bases)
+
+
+def test_every_declared_symbol_is_exported():
+    from blamm_gb300._native import gpu_lib, host_lib
+    for header, lib in (("blamm_gpu.h", gpu_lib()), ("blamm_host.h", host_lib())):
+        text = open(os.path.join(ROOT, "include", header)).read()
+        names = set(re.findall(r"^[A-Za-z_][\w \*]*?\b(blamm_\w+)\s*\(", text, flags=re.M))
+        assert len(names) > 5
+        for name in sorted(names):
+            assert hasattr(lib, name), f"{header}: {name} is not exported"
+
+
+def test_cli_errors_match_reference_behaviour(tmp_path):
+    """Host-side failures: missing files give a message and EXIT_FAILURE like the reference."""
+    import subprocess
+    d = gc.stage("cb", str(tmp_path))
+    r = subprocess.run([CLI_PATH, "dict", "missing.mf"], cwd=d, capture_output=True)
+    assert r.returncode == 1 and b"Could not open file: missing.mf" in r.stderr
+    r = subprocess.run([CLI_PATH, "hist", "motifs.cb", "sequences.mf"], cwd=d, capture_output=True)
+    assert r.returncode == 1 and b"Cannot open file: sequences.mf.dict" in r.stderr
+    r = subprocess.run([CLI_PATH, "scan", "-rt", "0.9", "-at", "3", "motifs.cb", "sequences.mf"], cwd=d,
+                       capture_output=True)
+    assert r.returncode == 1 and b"not both" in r.stderr
+    r = subprocess.run([CLI_PATH, "scan", "-pt", "2", "motifs.cb", "sequences.mf"], cwd=d, capture_output=True)
+    assert r.returncode == 1 and b"p-value should be in range" in r.stderr
+    with open(os.path.join(d, "bad.fa"), "w") as f:
+        f.write("ACGT\n>x\nACGT\n")
+    with open(os.path.join(d, "bad.mf"), "w") as f:
+        f.write("sp\tbad.fa\n")
+    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=d, capture_output=True)
+    assert r.returncode == 1 and b"does not appear to be in fasta format" in r.stderr
