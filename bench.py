@@ -72,18 +72,13 @@ def build_workload(seed: int, total: int):
     return wl, bases, runs, rseq, P, lens, thr
 
 
-def shard(bases, runs, rseq, rank, world):
-    """Contiguous share of the sequences for one rank (no data exchange)."""
+def shard(bases, runs, rank, world):
+    """Contiguous share of the stream for one rank, cut at run starts (no data exchange)."""
     if world == 1:
         return bases, runs
-    n = len(bases)
-    seq_ids = np.unique(rseq)
-    starts = np.array([runs[np.flatnonzero(rseq == s)[0]] for s in seq_ids] + [n])
-    targets = np.linspace(0, n, world + 1)
-    cut = [0] + [int(starts[np.argmin(np.abs(starts - t))]) for t in targets[1:-1]] + [n]
-    lo, hi = cut[rank], cut[rank + 1]
-    sel = (runs >= lo) & (runs < hi)
-    return bases[lo:hi], (runs[sel] - lo).astype(np.int64)
+    from blamm_gb300.shard import shard as cut
+    b, r, _ = cut(bases, runs, rank, world)
+    return b, r
 
 
 # ------------------------------------------------------------------ clocks
@@ -221,7 +216,7 @@ def run_ours(a, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     wl, bases_all, runs_all, rseq, P, lens, thr = build_workload(a.seed, a.bases)
-    bases, runs = shard(bases_all, runs_all, rseq, rank, world)
+    bases, runs = shard(bases_all, runs_all, rank, world)
     n, ncols = len(bases), P.shape[0]
     units = n * ncols
     flops_per_bp = float(8 * lens.astype(np.int64).sum())

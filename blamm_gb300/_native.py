@@ -74,10 +74,13 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_device_count.argtypes = [C.POINTER(C.c_int)]
     lib.blamm_set_softmask.argtypes = [vp, C.c_int]
     lib.blamm_score_histograms.argtypes = [vp, vp, i64, vp, i64, vp, vp, C.c_int, vp]
+    lib.blamm_debug_profile.argtypes = [vp, C.c_int]
+    lib.blamm_debug_profile_read.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
-                 "blamm_set_softmask", "blamm_score_histograms"):
+                 "blamm_set_softmask", "blamm_score_histograms", "blamm_debug_profile",
+                 "blamm_debug_profile_read"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -180,6 +183,17 @@ class GpuScanner:
         self._check(self.lib.blamm_score_histograms(self.h, _ptr(b), len(b), _ptr(runs), len(runs), _ptr(mn),
                                                     _ptr(w), nbins, _ptr(out)))
         return out
+
+    def profile(self, enable: bool) -> None:
+        self._check(self.lib.blamm_debug_profile(self.h, int(enable)))
+
+    def profile_read(self) -> np.ndarray:
+        """Per-CTA role timing of the last tensor-core scan, shape (ctas, 32)."""
+        n = C.c_int(0)
+        self._check(self.lib.blamm_debug_profile_read(self.h, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 32), dtype=np.int64)
+        self._check(self.lib.blamm_debug_profile_read(self.h, _ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
 
     def stats(self) -> dict:
         s = Stats()

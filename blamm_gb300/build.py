@@ -61,7 +61,7 @@ def _gpu_lib(force: bool) -> str:
     deps.append(os.path.join(INCLUDE, "blamm_gpu.h"))
     if force or _stale(out, deps):
         _run([_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-ffp-contract=off", "-shared", "-o", out,
+              "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-shared", "-o", out,
               os.path.join(CSRC, "blamm_gpu.cu"), "-lcudart"])
     return out
 

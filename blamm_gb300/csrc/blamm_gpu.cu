@@ -15,8 +15,9 @@
 #include <string>
 #include <vector>
 
-#include "../../include/blamm_gpu.h"
+#include "blamm_gpu.h"
 #include "scan_kernels.cuh"
+#include "scan_tc.cuh"
 
 using namespace blamm;
 
@@ -47,12 +48,12 @@ struct blamm_ctx {
     int plan_terms = 0;
     bool plan_valid = false;
     std::vector<TileDesc> tiles;
-    std::vector<float> guard;  // per column
-    int nslots = 0, wrows = 0;
+    std::vector<float> guard;    // per column
+    std::vector<double> bias_T;  // per column: threshold - guard on the column grid
+    int erows = 0;  // one-hot pair entries per E stage
     uint32_t b_term_max = 0, tmem_cols = 0;
     TileDesc *d_tiles = nullptr;
     uint8_t *d_bbuf = nullptr;
-    float *d_thr_adj = nullptr;
     int32_t *d_slot_col = nullptr;
 
     // stream buffers
@@ -68,6 +69,10 @@ struct blamm_ctx {
     int64_t hits_cap = 0;
     unsigned long long *d_counters = nullptr;  // [0] candidates, [1] hits
     int *d_status = nullptr;
+    bool prof_on = false;
+    long long *d_prof = nullptr;
+    std::vector<long long> prof;  // last scan's role timing, 16 per CTA
+    int prof_ctas = 0;
 
     blamm_stats stats{};
 };
@@ -139,14 +144,6 @@ inline uint16_t bf16_bits_exact(double v)
     return (uint16_t)(u >> 16);  // exact: v has <= 8 significant bits
 }
 
-float round_down_float(double t)
-{
-    if (std::isnan(t)) return std::numeric_limits<float>::infinity();
-    float f = (float)t;
-    if ((double)f > t) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
-    return f;
-}
-
 }  // namespace
 
 static int build_plan(blamm_ctx *ctx, int terms)
@@ -163,14 +160,17 @@ static int build_plan(blamm_ctx *ctx, int terms)
                      [&](int a, int b) { return ctx->len[a] < ctx->len[b]; });
 
     const int gmax_all = std::max(1, (ctx->lmax + 3) / 4);
-    const int wrows_all = kBM + 8 * (((gmax_all + 1) / 2) - 1);
+    const int erows_all = kBM + 4 * gmax_all + 8;
     const long long smem_limit = (long long)ctx->max_smem;
-    const long long other = 2LL * wrows_all * kWRowBytes + (long long)(ncols + 32 * (ncols / 32 + 16)) * 4 +
-                            4LL * kCandBuf * 8 + wrows_all + 64 + 64LL * sizeof(TileDesc) + 400 + 256 +
-                            2048;
+    // everything but the B tiles (W stages, bias A tile, candidate staging, ...)
+    const long long other = (long long)kEStages * erows_all * 16 + 4096 +
+                            (long long)kCodeStages * (code_seq_bytes(erows_all) + code_zm_bytes(erows_all)) +
+                            (long long)kEpiWarps * kCandBuf * 8 + 256LL * sizeof(TileDesc) + 64 + 128 + 64 + 2048 +
+                            1024;
     const long long b_term_cap = (smem_limit - other) / terms;
+    // widest tile whose B terms (g motif k-steps + 1 bias k-step) fit shared memory
     auto nmax_for = [&](int g) {
-        long long n = b_term_cap / (32LL * g);
+        long long n = b_term_cap / (32LL * (g + 1));
         n = n / 32 * 32;
         return (int)std::min<long long>(256, n);
     };
@@ -178,8 +178,8 @@ static int build_plan(blamm_ctx *ctx, int terms)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "motif bank does not fit shared memory");
 
     // DP over sorted columns: tile = contiguous run of sorted columns.
-    // Per-job cycle model: MMA = terms*g*N/2, epilogue ~ 2.5*N, W build ~ 300,
-    // fixed overhead ~ 150.
+    // Per-job cycle model: MMA = (terms*g + 1)*N/2 (bias step included),
+    // epilogue ~ N (8 warps, sign tests), W build ~ 300, fixed overhead ~ 200.
     const double kInf = 1e300;
     std::vector<double> f(ncols + 1, kInf);
     std::vector<int> from(ncols + 1, -1);
@@ -190,8 +190,8 @@ static int build_plan(blamm_ctx *ctx, int terms)
             const int g = std::max(1, (L + 3) / 4);
             const int N = (j - i + 31) / 32 * 32;
             if (N > nmax_for(g)) break;
-            const double mma = terms * g * N / 2.0, epi = 2.5 * N;
-            const double cost = std::max(std::max(mma, epi), 300.0) + 150.0;
+            const double mma = (terms * g + 1) * N / 2.0, epi = 1.0 * N;
+            const double cost = std::max(std::max(mma, epi), 300.0) + 200.0;
             if (f[i] + cost < f[j]) {
                 f[j] = f[i] + cost;
                 from[j] = i;
@@ -233,11 +233,15 @@ static int build_plan(blamm_ctx *ctx, int terms)
         ctx->guard[c] = (float)guard_d[c];
     }
 
-    // tiles, slots, B buffer
+    // tiles, slots, B buffer.  B term layout (canonical no-swizzle K-major):
+    // element (column i, K index kk) of a tile with g motif k-steps sits at
+    // ((i/8 * 2(g+1) + kk/8) * 8 + i%8) * 8 + kk%8; k-step g (K indices
+    // 16g..16g+15) holds, in the hi term, the bias: -T split into three
+    // BF16-exact pieces on the column's grid.
     std::vector<TileDesc> tiles;
-    std::vector<float> thr_adj;
     std::vector<int32_t> slot_col;
     std::vector<uint8_t> bbuf;
+    ctx->bias_T.assign(ncols, 0.0);
     int gmax = 1;
     uint32_t btmax = 0;
     int nmax = 0;
@@ -250,35 +254,44 @@ static int build_plan(blamm_ctx *ctx, int terms)
         td.slot0 = (int32_t)slot_col.size();
         td.n = N;
         td.g = g;
-        td.b_bytes = N * 16 * g * 2;
+        td.b_bytes = N * 16 * (g + 1) * 2;
         size_t off = (bbuf.size() + 1023) / 1024 * 1024;
         td.b_off = (int64_t)off;
         bbuf.resize(off + (size_t)td.b_bytes * terms, 0);
+        uint16_t *b_hi = reinterpret_cast<uint16_t *>(bbuf.data() + off);
+        uint16_t *b_lo = terms == 2 ? reinterpret_cast<uint16_t *>(bbuf.data() + off + td.b_bytes) : nullptr;
+        auto elem = [&](int i, int kk) {
+            return ((size_t)((i / 8) * 2 * (g + 1) + kk / 8) * 8 + i % 8) * 8 + kk % 8;
+        };
         for (int i = 0; i < N; ++i) {
             const int c = i < cnt ? order[sp.first + i] : -1;
             slot_col.push_back(c);
-            if (c < 0) {
-                thr_adj.push_back(std::numeric_limits<float>::infinity());
-                continue;
+            // bias: T on the grid u = 2^-(k+8), clamped to +-2^23 u (a padding column
+            // gets T = 2^22 u at k = 0: never a candidate)
+            int k = 0;
+            int64_t Tint = (int64_t)1 << 22;
+            if (c >= 0) {
+                k = kcol[c];
+                const double t = ((double)ctx->thr[c] - guard_d[c]) * std::ldexp(1.0, k + 8);
+                const double lim = std::ldexp(1.0, 23);
+                Tint = std::isnan(t) ? (int64_t)lim : (int64_t)std::floor(std::max(-lim, std::min(lim, t)));
+                ctx->bias_T[c] = (double)Tint * std::ldexp(1.0, -(k + 8));
             }
-            thr_adj.push_back(round_down_float((double)ctx->thr[c] - guard_d[c]));
+            const int64_t pa = (int64_t)std::llround((double)Tint / 65536.0);
+            const int64_t rem = Tint - pa * 65536;
+            const int64_t pb = (int64_t)std::llround((double)rem / 256.0);
+            const int64_t pc = rem - pb * 256;
+            const int64_t pieces[3] = {pa * 65536, pb * 256, pc};
+            for (int s = 0; s < 3; ++s)
+                if (pieces[s] != 0) b_hi[elem(i, 16 * g + s)] = bf16_bits_exact(-std::ldexp((double)pieces[s], -(k + 8)));
+            if (c < 0) continue;
             const float *col = &ctx->P[(size_t)c * ctx->p_rows];
             const int Lc = ctx->len[c];
-            const int ng = i / 8, r = i % 8;
-            for (int kk = 0; kk < 16 * g; ++kk) {
-                const int j = kk / 4;
-                if (j >= Lc) break;
+            for (int kk = 0; kk < 4 * Lc; ++kk) {
                 const double v = col[kk];
-                const double hi = q_hi(v, kcol[c]);
-                const double lo = q_lo(v - hi, kcol[c]);
-                const int kc = kk / 8, e = kk % 8;
-                const size_t elem = ((size_t)(ng * 2 * g + kc) * 8 + r) * 8 + e;
-                uint16_t *b_hi = reinterpret_cast<uint16_t *>(bbuf.data() + off);
-                b_hi[elem] = bf16_bits_exact(hi);
-                if (terms == 2) {
-                    uint16_t *b_lo = reinterpret_cast<uint16_t *>(bbuf.data() + off + td.b_bytes);
-                    b_lo[elem] = bf16_bits_exact(lo);
-                }
+                const double hi = q_hi(v, k);
+                b_hi[elem(i, kk)] = bf16_bits_exact(hi);
+                if (b_lo) b_lo[elem(i, kk)] = bf16_bits_exact(q_lo(v - hi, k));
             }
         }
         tiles.push_back(td);
@@ -290,23 +303,18 @@ static int build_plan(blamm_ctx *ctx, int terms)
     // upload
     if (ctx->d_tiles) cudaFree(ctx->d_tiles);
     if (ctx->d_bbuf) cudaFree(ctx->d_bbuf);
-    if (ctx->d_thr_adj) cudaFree(ctx->d_thr_adj);
     if (ctx->d_slot_col) cudaFree(ctx->d_slot_col);
     ctx->d_tiles = nullptr;
     ctx->d_bbuf = nullptr;
-    ctx->d_thr_adj = nullptr;
     ctx->d_slot_col = nullptr;
     CK(cudaMalloc(&ctx->d_tiles, sizeof(TileDesc) * tiles.size()));
     CK(cudaMalloc(&ctx->d_bbuf, bbuf.size()));
-    CK(cudaMalloc(&ctx->d_thr_adj, sizeof(float) * thr_adj.size()));
     CK(cudaMalloc(&ctx->d_slot_col, sizeof(int32_t) * slot_col.size()));
     CK(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_bbuf, bbuf.data(), bbuf.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_thr_adj, thr_adj.data(), sizeof(float) * thr_adj.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_slot_col, slot_col.data(), sizeof(int32_t) * slot_col.size(), cudaMemcpyHostToDevice));
     ctx->tiles = tiles;
-    ctx->nslots = (int)slot_col.size();
-    ctx->wrows = kBM + 8 * (((gmax + 1) / 2) - 1);
+    ctx->erows = kBM + 4 * gmax + 8;
     ctx->b_term_max = btmax;
     ctx->tmem_cols = nmax <= 128 ? 256u : 512u;
     ctx->plan_terms = terms;
@@ -342,8 +350,13 @@ int blamm_ctx_create(int device, blamm_ctx **out)
         ctx->sm_count = prop.multiProcessorCount;
         ctx->max_smem = (int)prop.sharedMemPerBlockOptin;
         cudaFuncAttributes fa;
-        CK(cudaFuncGetAttributes(&fa, scan_tc_kernel));  // fails if no sm_103a image fits
-        CK(cudaFuncSetAttribute(scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CK(cudaFuncGetAttributes(&fa, scan_tc_kernel<false>));  // fails if no sm_103a image fits
+        if (fa.maxThreadsPerBlock < kTcThreads)
+            return fail(ctx, BLAMM_ERR_UNSUPPORTED, "scan kernel: %d registers allow only %d threads per block (< %d)",
+                        fa.numRegs, fa.maxThreadsPerBlock, kTcThreads);
+        CK(cudaFuncSetAttribute(scan_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                ctx->max_smem));
+        CK(cudaFuncSetAttribute(scan_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 ctx->max_smem));
         CK(cudaFuncSetAttribute(scan_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 ctx->max_smem));
@@ -369,7 +382,7 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     void *bufs[] = {ctx->d_P,      ctx->d_len,   ctx->d_thr,      ctx->d_tiles, ctx->d_bbuf,
-                    ctx->d_thr_adj, ctx->d_slot_col, ctx->d_bases, ctx->d_seq2, ctx->d_zmask,
+                    ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask,
                     ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status};
     for (void *b : bufs)
         if (b) cudaFree(b);
@@ -479,7 +492,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         if (rc) return rc;
         ctx->cand_cap = (int64_t)cap;
     }
-    const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->wrows, ctx->nslots,
+    const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows,
                                     (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
@@ -497,10 +510,8 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         p.ntiles = (int32_t)ctx->tiles.size();
         p.terms = ctx->plan_terms;
         p.bbuf = ctx->d_bbuf;
-        p.thr_adj = ctx->d_thr_adj;
         p.slot_col = ctx->d_slot_col;
-        p.nslots = ctx->nslots;
-        p.wrows = ctx->wrows;
+        p.erows = ctx->erows;
         p.b_term_max = ctx->b_term_max;
         p.tmem_cols = ctx->tmem_cols;
         p.cand = ctx->d_cand;
@@ -512,10 +523,17 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         p.dump_p0 = dump_p0;
         p.dump_npos = dump_npos;
         p.dump_ncols = ctx->ncols;
+        p.prof = nullptr;
+        if (ctx->prof_on) {
+            if (!ctx->d_prof) CK(cudaMalloc(&ctx->d_prof, sizeof(long long) * 32 * ctx->sm_count));
+            CK(cudaMemsetAsync(ctx->d_prof, 0, sizeof(long long) * 32 * ctx->sm_count, ctx->stream));
+            p.prof = ctx->d_prof;
+        }
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
         if (njobs > 0) {
             CK(cudaEventRecord(ctx->ev[4], ctx->stream));
-            scan_tc_kernel<<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            if (dump) scan_tc_kernel<true><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            else scan_tc_kernel<false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
             CK(cudaGetLastError());
             CK(cudaEventRecord(ctx->ev[5], ctx->stream));
             ++*launches;
@@ -527,6 +545,11 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         CK(cudaStreamSynchronize(ctx->stream));
         if (status) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
         if (njobs > 0) cudaEventElapsedTime(&ctx->stats.scan_ms, ctx->ev[4], ctx->ev[5]);
+        if (ctx->prof_on && njobs > 0) {
+            ctx->prof.resize((size_t)32 * grid);
+            CK(cudaMemcpy(ctx->prof.data(), ctx->d_prof, sizeof(long long) * 32 * grid, cudaMemcpyDeviceToHost));
+            ctx->prof_ctas = grid;
+        }
         ctx->stats.candidates = (int64_t)ncand;
         if ((int64_t)ncand <= ctx->cand_cap) break;
         // grow and re-run
@@ -541,6 +564,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     }
     RescoreParams r{};
     r.cand = ctx->d_cand;
+    r.slot_col = ctx->d_slot_col;
     r.cand_count = ctx->d_counters;
     r.cand_cap = ctx->cand_cap;
     r.seq2 = ctx->d_seq2;
@@ -807,6 +831,22 @@ int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const i
     return BLAMM_OK;
 }
 
+int blamm_debug_profile(blamm_ctx *ctx, int enable)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    ctx->prof_on = enable != 0;
+    return BLAMM_OK;
+}
+
+int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, int *nctas)
+{
+    if (!ctx || !nctas) return BLAMM_ERR_ARG;
+    *nctas = ctx->prof_ctas;
+    if (out)
+        for (int i = 0; i < 32 * std::min(max_ctas, ctx->prof_ctas); ++i) out[i] = ctx->prof[(size_t)i];
+    return BLAMM_OK;
+}
+
 int blamm_ctx_stream(const blamm_ctx *ctx, void **stream)
 {
     if (!ctx || !stream) return BLAMM_ERR_ARG;
@@ -864,6 +904,12 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
                                         cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
+        // the accumulator holds sum(q) - T; report sum(q) (exact: both are on the column grid)
+        for (int64_t i = 0; rc == BLAMM_OK && i < npos; ++i)
+            for (int c = 0; c < ctx->ncols; ++c) {
+                float &v = out[i * ctx->ncols + c];
+                v = (float)((double)v + ctx->bias_T[c]);
+            }
     }
     cudaFree(d_dump);
     return rc;

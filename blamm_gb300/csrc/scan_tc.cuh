@@ -1,0 +1,556 @@
+// scan_tc.cuh -- the fused tensor-core PWM scan (tcgen05 + TMA bulk + TMEM),
+// one persistent CTA per SM.
+//
+// Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
+// For an M tile of 128 positions starting at m0, the W-builder warp writes
+// one 16-byte entry per position, E[i] = onehot(base m0+i) ++ onehot(base
+// m0+i+1) (2 bases x 4 channels x bf16).  Read with row stride 16 B, 8-row
+// group stride (SBO) 128 B and K-core stride (LBO) 32 B, the entries starting
+// at E[4g] form exactly the A operand of motif bases 4g..4g+3 for all 128
+// positions -- the overlapping one-hot windows of the reference's S matrix
+// (src/sequence.cpp:299-340) without materialising them: each k-step is a
+// shifted A descriptor over the same ~150 entries.  B_g holds rows
+// 16g..16g+15 of P for the tile's columns.
+//
+// Arithmetic.  Column c's P enters as fixed-point BF16 terms: hi on the grid
+// 2^-k, lo on 2^-(k+8), k = 7 - ceil(log2 max|P_c|), so |hi| <= 128 * 2^-k.
+// The accumulator starts at -T (one extra "bias" MMA: a constant A tile with
+// 1.0 in K slots 0-2 times three BF16 pieces of T), where T is the column's
+// threshold minus its guard band, rounded down to the grid u = 2^-(k+8).
+// Every partial sum is then an integer multiple of u below 2^24 u in
+// magnitude (motifs up to 256 long), i.e. exactly representable in FP32: the
+// accumulator holds sum(q) - T exactly, whatever the tensor cores' internal
+// rounding, and a position is a candidate iff its sign bit is clear.  The
+// guard band bounds |sum(q) - sum(P)| plus the reference's own FP32 rounding
+// of sum(P), so every reference hit is a candidate; candidates are rescored
+// in exact FP32 (rescore_kernel).
+//
+// Roles (640 threads): warps 0-15 drain TMEM (lane quarter = warp % 4, column
+// group = warp / 4) and test sign bits; warp 16 allocates TMEM and one lane
+// issues the MMAs and the TMA bulk copies of B tiles; warp 17 builds E from
+// 2-bit code windows that it prefetches with TMA bulk copies kCodeStages jobs
+// ahead.  Two E stages and two TMEM accumulators keep the roles overlapped.
+// Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
+// major, so a CTA reloads B only when its tile changes.  Every wait is
+// bounded: on a timeout the CTA raises an abort flag, every role stops,
+// outstanding MMAs are drained and TMEM is freed.
+#pragma once
+#include <cstdint>
+
+#include "ptx_sm100.cuh"
+#include "scan_kernels.cuh"
+
+namespace blamm {
+
+constexpr int kBM = 128;         // positions per M tile (= UMMA M)
+constexpr int kMaxTcLen = 256;   // longest motif on the tensor-core path
+constexpr int kCandBuf = 128;    // per-warp staging of candidates in SMEM
+constexpr int kEpiWarps = 16;    // TMEM drain warps (4 per lane quarter)
+constexpr int kMmaWarp = 16;
+constexpr int kWWarp = 17;
+constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps); 18 and 19 idle
+constexpr int kCodeStages = 4;   // code windows in flight
+constexpr int kEStages = 4;      // one-hot E stages
+
+// Per-N-tile description (host-built, staged in SMEM by the kernel).
+struct TileDesc {
+    int32_t slot0;    // first column slot of the tile (slots: tile-local padded columns)
+    int32_t n;        // UMMA N: columns of the tile, padded to a multiple of 32 (<= 256)
+    int32_t g;        // k-steps of motif data: ceil(max motif length in the tile / 4)
+    int32_t b_bytes;  // bytes of one B term: n x 16 x (g + 1) bf16 (last k-step: bias)
+    int64_t b_off;    // byte offset of the tile's first B term in the B buffer
+    int64_t pad;
+};
+
+struct TcParams {
+    const uint32_t *seq2;
+    const uint32_t *zmask;
+    int64_t n;           // stream positions
+    int64_t n_mtiles;    // ceil(n / 128)
+    const TileDesc *tiles;
+    int32_t ntiles;
+    int32_t terms;       // 1 (hi) or 2 (hi + lo)
+    const uint8_t *bbuf; // B tiles
+    const int32_t *slot_col;  // per slot: motif column, -1 for padding
+    int32_t erows;       // E entries per stage (128 + 4 * max k-steps + 8)
+    uint32_t b_term_max; // bytes reserved per B term in SMEM
+    uint32_t tmem_cols;  // TMEM columns allocated (2 accumulators)
+    unsigned long long *cand;
+    unsigned long long *cand_count;
+    int64_t cand_cap;
+    int *status;         // bit 0: a device wait timed out
+    long long wait_limit;  // clock64 cycles a wait may last
+    // debug dump of the accumulator, sum(q) - T (positions [dump_p0, dump_p0+dump_npos))
+    float *dump;
+    int64_t dump_p0, dump_npos;
+    int32_t dump_ncols;
+    // optional per-CTA role timing (32 counters per CTA, clock64 cycles): see tc_prof_fields
+    long long *prof;
+};
+
+// tc_prof_fields: 0 MMA wait acc_empty, 1 MMA wait E full, 2 MMA B reloads, 3 MMA loop,
+// 4 E wait code window, 5 E wait E empty, 6 E loop, 7 epilogue wait acc_full,
+// 8 epilogue loop, 9 epilogue drain (acc_full -> acc_empty arrive), 10 jobs,
+// 11 E-builder build time, 12 epilogue rounds with a candidate, 16-23 drain time of
+// epilogue warps 0-7, 24-31 their accumulator waits
+
+// bytes of one prefetched code window (2-bit codes and zero mask) for erows entries
+__host__ __device__ inline uint32_t code_seq_bytes(int erows) { return (uint32_t)(((erows + 2 + 15) / 16 * 4 + 15) / 16 * 16); }
+__host__ __device__ inline uint32_t code_zm_bytes(int erows) { return (uint32_t)(((erows + 2 + 31) / 32 * 4 + 15) / 16 * 16); }
+
+struct TcSmem {
+    // byte offsets into dynamic shared memory
+    uint32_t b_hi, b_lo, e0, abias, codes, cand, tiles, bars, misc, total;
+};
+
+__host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms, int erows, int ntiles)
+{
+    TcSmem L;
+    uint32_t o = 0;
+    auto take = [&](uint32_t bytes, uint32_t align) {
+        o = (o + align - 1) / align * align;
+        uint32_t r = o;
+        o += bytes;
+        return r;
+    };
+    L.b_hi = take(b_term_max, 1024);
+    L.b_lo = take(terms == 2 ? b_term_max : 0, 1024);
+    L.e0 = take((uint32_t)kEStages * erows * 16, 128);  // kEStages stages of erows entries
+    L.abias = take(16 * 256, 128);  // 128 rows x 16 K-elements, canonical K-major layout
+    L.codes = take(kCodeStages * (code_seq_bytes(erows) + code_zm_bytes(erows)), 128);
+    L.cand = take(kEpiWarps * kCandBuf * 8, 16);
+    L.tiles = take((uint32_t)ntiles * sizeof(TileDesc), 16);
+    L.bars = take(32 * 8, 8);
+    L.misc = take(64, 16);
+    L.total = take(0, 1024) + 1024;  // + slack for aligning the runtime base
+    return L;
+}
+
+enum {
+    BAR_WFULL = 0,   // E stage built        (kEStages)
+    BAR_WEMPTY = 4,  // E stage consumed     (kEStages)
+    BAR_AFULL = 8,   // accumulator ready    (2)
+    BAR_AEMPTY = 10, // accumulator drained  (2)
+    BAR_BFULL = 12,  // B tile landed
+    BAR_DRAIN = 13,  // MMAs drained
+    BAR_CODE = 14    // code window landed   (kCodeStages)
+};
+
+// AND of 32 words as a shallow tree (3-input LOPs)
+__device__ __forceinline__ uint32_t and32(const uint32_t (&v)[32])
+{
+    uint32_t t[11];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) t[i] = v[3 * i] & v[3 * i + 1] & v[3 * i + 2];
+    t[10] = v[30] & v[31];
+    const uint32_t a = t[0] & t[1] & t[2], b = t[3] & t[4] & t[5], c = t[6] & t[7] & t[8];
+    return (a & b & c) & (t[9] & t[10]);
+}
+
+// The jobs of one CTA: job = blockIdx.x + k * gridDim.x, tile = job / n_mtiles,
+// m = job % n_mtiles, advanced without 64-bit divisions after the first.
+struct JobIter {
+    long long job;
+    int tile;
+    int64_t m;
+    __device__ __forceinline__ void init(long long j, int64_t n_mtiles)
+    {
+        job = j;
+        tile = (int)(j / n_mtiles);
+        m = j % n_mtiles;
+    }
+    __device__ __forceinline__ void next(int stride, int64_t n_mtiles)
+    {
+        job += stride;
+        m += stride;
+        while (m >= n_mtiles) {
+            m -= n_mtiles;
+            ++tile;
+        }
+    }
+};
+
+// Write a warp's staged candidates to the global candidate list (one atomic per warp).
+__device__ __noinline__ int flush_candidates(int lane, unsigned long long *buf, int fill, unsigned long long *cand,
+                                             unsigned long long *cand_count, int64_t cand_cap)
+{
+    __syncwarp();
+    unsigned long long gb = 0;
+    if (lane == 0 && fill > 0) gb = atomicAdd(cand_count, (unsigned long long)fill);
+    gb = __shfl_sync(0xffffffffu, gb, 0);
+    for (int i = lane; i < fill; i += 32)
+        if ((int64_t)(gb + i) < cand_cap) cand[gb + i] = buf[i];
+    __syncwarp();
+    return 0;
+}
+
+// Stage the candidates of one 32-column chunk (mask bit i = column slot0 + i of this
+// lane's position) in the warp's SMEM buffer; returns the new fill.  Warp-collective.
+__device__ __forceinline__ int stage_candidates(uint32_t mask, int slot0, int64_t pos, int lane, unsigned long long *buf,
+                                             int fill, unsigned long long *cand, unsigned long long *cand_count,
+                                             int64_t cand_cap)
+{
+    const int cnt = __popc(mask);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return fill;
+    int at = incl - cnt;
+    if (fill + total > kCandBuf) fill = flush_candidates(lane, buf, fill, cand, cand_count, cand_cap);
+    const unsigned long long key = (unsigned long long)pos << kColBits;
+    if (total > kCandBuf) {  // more than a buffer: straight to global memory
+        unsigned long long gb = 0;
+        if (lane == 0) gb = atomicAdd(cand_count, (unsigned long long)total);
+        gb = __shfl_sync(0xffffffffu, gb, 0);
+        while (mask) {
+            const int i = __ffs(mask) - 1;
+            mask &= mask - 1;
+            if ((int64_t)(gb + at) < cand_cap) cand[gb + at] = key | (unsigned long long)(slot0 + i);
+            ++at;
+        }
+        __syncwarp();
+        return fill;
+    }
+    while (mask) {
+        const int i = __ffs(mask) - 1;
+        mask &= mask - 1;
+        buf[fill + at] = key | (unsigned long long)(slot0 + i);
+        ++at;
+    }
+    __syncwarp();
+    return fill + total;
+}
+
+template <bool kDump>
+__global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + ((1024 - (ptx::smem_addr(smem_raw) & 1023)) & 1023);
+    const TcSmem L = tc_smem_layout(p.b_term_max, p.terms, p.erows, p.ntiles);
+    const uint32_t sbase = ptx::smem_addr(smem);
+    unsigned long long *s_cand = reinterpret_cast<unsigned long long *>(smem + L.cand);
+    TileDesc *s_tiles = reinterpret_cast<TileDesc *>(smem + L.tiles);
+    const uint32_t bars = sbase + L.bars;
+    volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L.misc);
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(smem + L.misc + 4);
+    const uint32_t seq_bytes = code_seq_bytes(p.erows), zm_bytes = code_zm_bytes(p.erows);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // ---- set-up
+    for (int i = threadIdx.x; i < p.ntiles * (int)(sizeof(TileDesc) / 4); i += blockDim.x)
+        reinterpret_cast<int32_t *>(s_tiles)[i] = reinterpret_cast<const int32_t *>(p.tiles)[i];
+    {
+        // constant A of the bias MMA: every row = [1, 1, 1, 0, ...] (16 K slots)
+        uint4 *ab = reinterpret_cast<uint4 *>(smem + L.abias);
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) {  // 16 row groups x 2 cores x 8 rows
+            const int core = (i >> 3) & 1;
+            ab[i] = core == 0 ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    if (threadIdx.x == 0) {
+        *s_abort = 0;
+        for (int s = 0; s < kEStages; ++s) {
+            ptx::mbar_init(bars + 8 * (BAR_WFULL + s), 1);
+            ptx::mbar_init(bars + 8 * (BAR_WEMPTY + s), 1);
+        }
+        for (int s = 0; s < 2; ++s) {
+            ptx::mbar_init(bars + 8 * (BAR_AFULL + s), 1);
+            ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps);
+        }
+        ptx::mbar_init(bars + 8 * BAR_BFULL, 1);
+        ptx::mbar_init(bars + 8 * BAR_DRAIN, 1);
+        for (int s = 0; s < kCodeStages; ++s) ptx::mbar_init(bars + 8 * (BAR_CODE + s), 1);
+        ptx::fence_mbar_init();
+    }
+    if (warp == kMmaWarp) {
+        ptx::tmem_alloc(ptx::smem_addr(s_tmem), p.tmem_cols);
+        ptx::tmem_relinquish();
+        ptx::tc_fence_before();
+    }
+    ptx::fence_proxy_async_smem();  // the bias A tile is read by the tensor cores
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem_base = *s_tmem;
+    const uint32_t acc_stride = p.tmem_cols >> 1;
+    const long long njobs = (long long)p.ntiles * p.n_mtiles;
+
+    if (warp == kMmaWarp) {
+        // =========================== MMA issuer ===========================
+        if (lane == 0) {
+            int cur_tile = -1;
+            uint32_t bphase = 0, dphase = 0, idesc = 0, g_steps = 0, sbo_b = 0;
+            long long t_acc = 0, t_w = 0, t_b = 0;
+            const long long t_start = clock64();
+            const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
+            uint32_t jc = 0;
+            bool ok = true;
+            JobIter it;
+            for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
+                const int tile = it.tile;
+                if (tile != cur_tile) {
+                    const long long tb = clock64();
+                    if (cur_tile >= 0) {  // every MMA reading the old B must be done
+                        ptx::mma_commit(bars + 8 * BAR_DRAIN);
+                        ok = ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit);
+                        dphase ^= 1;
+                        if (!ok) break;
+                    }
+                    const TileDesc td = s_tiles[tile];
+                    ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * p.terms);
+                    ptx::bulk_g2s(sbase + L.b_hi, p.bbuf + td.b_off, (uint32_t)td.b_bytes,
+                                  bars + 8 * BAR_BFULL);
+                    if (p.terms == 2)
+                        ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes,
+                                      (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
+                    ok = ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit);
+                    bphase ^= 1;
+                    if (!ok) break;
+                    cur_tile = tile;
+                    if (p.prof) t_b += clock64() - tb;
+                    g_steps = (uint32_t)td.g;
+                    idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
+                    sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
+                }
+                const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;                   // accumulator
+                const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
+                const long long t0 = clock64();
+                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
+                const long long t1 = clock64();
+                ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
+                if (p.prof) {
+                    t_acc += t1 - t0;
+                    t_w += clock64() - t1;
+                }
+                if (!ok) break;
+                ptx::tc_fence_after();
+                const uint32_t d_tmem = tmem_base + s * acc_stride;
+                const uint32_t e_addr = sbase + L.e0 + es * (uint32_t)p.erows * 16u;
+                // D = -T (bias pieces in the last k-step of the hi term)
+                ptx::mma_bf16(d_tmem, adesc_bias, ptx::smem_desc(sbase + L.b_hi + g_steps * 256u, 128u, sbo_b),
+                              idesc, 0u);
+                for (uint32_t g = 0; g < g_steps; ++g) {
+                    // A: entries 4g .. 4g+129 (rows 16 B apart, row groups 128 B, K cores 32 B)
+                    const uint64_t adesc = ptx::smem_desc(e_addr + 64u * g, 32u, 128u);
+                    ptx::mma_bf16(d_tmem, adesc, ptx::smem_desc(sbase + L.b_hi + g * 256u, 128u, sbo_b), idesc, 1u);
+                    if (p.terms == 2)
+                        ptx::mma_bf16(d_tmem, adesc, ptx::smem_desc(sbase + L.b_lo + g * 256u, 128u, sbo_b), idesc,
+                                      1u);
+                }
+                ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
+                ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
+            }
+            // drain: nothing may still write TMEM when it is freed
+            ptx::mma_commit(bars + 8 * BAR_DRAIN);
+            if (!ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit)) *s_abort = 1;
+            if (p.prof) {
+                long long *pr = p.prof + 32 * blockIdx.x;
+                pr[0] = t_acc;
+                pr[1] = t_w;
+                pr[2] = t_b;
+                pr[3] = clock64() - t_start;
+                pr[10] = jc;
+            }
+        }
+        __syncwarp();
+    } else if (warp == kWWarp) {
+        // ========================== E builder =============================
+        const uint32_t codes = sbase + L.codes;
+        JobIter ahead;  // the job whose code window is fetched next
+        ahead.init(blockIdx.x, p.n_mtiles);
+        auto fetch = [&](uint32_t jc) {  // lane 0: code window of the jc-th job into its ring stage
+            if (ahead.job >= njobs) return;
+            const int64_t m = ahead.m;
+            ahead.next(gridDim.x, p.n_mtiles);
+            const uint32_t st = jc % kCodeStages;
+            const uint32_t dst = codes + st * (seq_bytes + zm_bytes);
+            ptx::mbar_arrive_expect_tx(bars + 8 * (BAR_CODE + st), seq_bytes + zm_bytes);
+            ptx::bulk_g2s(dst, p.seq2 + m * (kBM / 16), seq_bytes, bars + 8 * (BAR_CODE + st));
+            ptx::bulk_g2s(dst + seq_bytes, p.zmask + m * (kBM / 32), zm_bytes, bars + 8 * (BAR_CODE + st));
+        };
+        if (lane == 0)
+            for (uint32_t j = 0; j < kCodeStages; ++j) fetch(j);
+        long long t_code = 0, t_we = 0, t_build = 0;
+        const long long t_start = clock64();
+        uint32_t jc = 0;
+        JobIter it;
+        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
+            const int tile = it.tile;
+            const int g = s_tiles[tile].g;
+            const int entries = kBM + 4 * g + 2;
+            const uint32_t cs = jc % kCodeStages, cph = (jc / kCodeStages) & 1u;
+            const uint32_t s = jc % kEStages, ph = (jc / kEStages) & 1u;
+            const long long t0 = clock64();
+            if (!ptx::mbar_wait(bars + 8 * (BAR_CODE + cs), cph, s_abort, p.wait_limit)) break;
+            const long long t1 = clock64();
+            if (!ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit)) break;
+            if (p.prof) {
+                t_code += t1 - t0;
+                t_we += clock64() - t1;
+            }
+            const uint32_t *cw = reinterpret_cast<const uint32_t *>(smem + L.codes + cs * (seq_bytes + zm_bytes));
+            const uint32_t *zw = cw + seq_bytes / 4;
+            uint4 *e = reinterpret_cast<uint4 *>(smem + L.e0 + s * (uint32_t)p.erows * 16u);
+            // one-hot of a base as 4 bf16 channels in two words: 1.0 (0x3F80) in half
+            // (code & 1) of word (code >> 1); a zero-masked base gives zeros
+            auto onehot = [](uint32_t code, uint32_t zero) {
+                const uint32_t h = zero ? 0u : (0x3F80u << ((code & 1u) << 4));
+                return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
+            };
+            const long long t2 = clock64();
+#pragma unroll 4
+            for (int i = lane; i < entries; i += 32) {
+                const int j = i + 1;
+                const uint2 a = onehot((cw[i >> 4] >> (2 * (i & 15))) & 3u, (zw[i >> 5] >> (i & 31)) & 1u);
+                const uint2 b = onehot((cw[j >> 4] >> (2 * (j & 15))) & 3u, (zw[j >> 5] >> (j & 31)) & 1u);
+                e[i] = make_uint4(a.x, a.y, b.x, b.y);
+            }
+            __syncwarp();
+            if (p.prof) t_build += clock64() - t2;
+            if (lane == 0) {
+                ptx::fence_proxy_async_smem();  // the generic reads of stage cs precede its refill
+                fetch(jc + kCodeStages);
+            }
+            ptx::fence_proxy_async_smem();  // E is read by the tensor cores
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
+        }
+        if (p.prof && lane == 0) {
+            long long *pr = p.prof + 32 * blockIdx.x;
+            pr[4] = t_code;
+            pr[5] = t_we;
+            pr[11] = t_build;
+        }
+        // a prefetched window may still be in flight when the loop ends early
+        if (lane == 0)
+            for (uint32_t j = jc; j < jc + kCodeStages; ++j) {
+                const long long job = blockIdx.x + (long long)j * gridDim.x;
+                if (job >= njobs || *s_abort == 0) break;
+                ptx::mbar_wait(bars + 8 * (BAR_CODE + j % kCodeStages), (j / kCodeStages) & 1u, s_abort,
+                               p.wait_limit);
+            }
+    } else if (warp < kEpiWarps) {
+        // ===================== epilogue (warps 0-15) ======================
+        const int q = warp & 3;     // TMEM lanes 32q .. 32q+31
+        const int grp = warp >> 2;  // 32-column chunks grp, grp + 4
+        unsigned long long *buf = s_cand + warp * kCandBuf;
+        int fill = 0;
+        long long t_af = 0, t_dr = 0, n_rare = 0, t_ld = 0, t_f1 = 0, t_red = 0, t_f2 = 0;
+        const long long t_start = clock64();
+        uint32_t jc = 0;
+        JobIter it;
+        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
+            const int tile = it.tile;
+            const int64_t m = it.m;
+            const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
+            const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;
+            const long long t0 = clock64();
+            if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
+            const long long t1 = clock64();
+            if (p.prof) t_af += t1 - t0;
+            ptx::tc_fence_after();
+            if (p.prof) t_f1 += clock64() - t1;
+            const int64_t pos = m * kBM + q * 32 + lane;
+            const bool valid = pos < p.n;
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + s * acc_stride;
+            const bool dump_row = kDump && pos >= p.dump_p0 && pos < p.dump_p0 + p.dump_npos;
+            // This warp's 32-column chunks grp and grp+4 (N <= 256) in one round of two
+            // TMEM loads, AND-reduced to one word whose sign bit is clear iff some column
+            // is a candidate, and only then (rare) turned into masks.  The accumulator is
+            // handed back after the reduction; staging comes after that.
+            uint32_t msk[2] = {0u, 0u};
+            bool anyw = false;
+#pragma unroll
+            for (int round = 0; round < 1; ++round) {
+                const int ca = grp, cb = grp + 4;
+                if (ca >= nch) break;  // warp-uniform
+                uint32_t va[32], vb[32];
+                const long long tl0 = clock64();
+                ptx::tmem_ld_32x32b_x32(taddr + ca * 32, va);
+                if (cb < nch) ptx::tmem_ld_32x32b_x32(taddr + cb * 32, vb);
+                ptx::tmem_wait_ld();
+                ptx::reg_fence(va);
+                ptx::reg_fence(vb);
+                const long long tr0 = clock64();
+                const uint32_t r = cb < nch ? (and32(va) & and32(vb)) : and32(va);
+                const bool any = valid && (int32_t)r >= 0;
+                if (__any_sync(0xffffffffu, any)) {
+                    anyw = true;
+                    if (any) {
+                        uint32_t m0 = 0, m1 = 0;
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) {
+                            m0 |= ((~va[i]) >> 31) << i;
+                            m1 |= ((~vb[i]) >> 31) << i;
+                        }
+                        msk[0] = m0;
+                        msk[1] = cb < nch ? m1 : 0u;
+                    }
+                }
+                if (kDump && dump_row) {  // debug instantiation only: raw accumulator of some positions
+                    float *row = p.dump + (pos - p.dump_p0) * p.dump_ncols;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        int col = __ldg(p.slot_col + slot0 + ca * 32 + i);
+                        if (col >= 0) row[col] = __uint_as_float(va[i]);
+                        if (cb < nch && (col = __ldg(p.slot_col + slot0 + cb * 32 + i)) >= 0)
+                            row[col] = __uint_as_float(vb[i]);
+                    }
+                }
+                if (p.prof) {
+                    const long long tr1 = clock64();
+                    t_ld += tr0 - tl0;
+                    t_red += tr1 - tr0;
+                }
+            }
+            const long long tf0 = clock64();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
+            if (p.prof) {
+                const long long tf1 = clock64();
+                t_f2 += tf1 - tf0;
+                t_dr += tf1 - t1;
+            }
+            if (anyw) {  // rare: stage this lane's candidates
+                ++n_rare;
+#pragma unroll
+                for (int k = 0; k < 2; ++k)
+                    fill = stage_candidates(msk[k], slot0 + (grp + 4 * k) * 32, pos, lane, buf, fill, p.cand,
+                                            p.cand_count, p.cand_cap);
+            }
+        }
+        fill = flush_candidates(lane, buf, fill, p.cand, p.cand_count, p.cand_cap);
+        if (p.prof && lane == 0) {
+            long long *pr = p.prof + 32 * blockIdx.x;
+            if (warp == 0) {
+                pr[7] = t_af;
+                pr[8] = clock64() - t_start;
+                pr[9] = t_dr;
+                pr[12] = n_rare;
+                pr[13] = t_ld;
+                pr[14] = t_f1;
+                pr[15] = t_red;
+                pr[6] = t_f2;
+            }
+            if (warp < 8) {  // counters 16..31 hold warps 0-7 only
+                pr[16 + warp] = t_dr;
+                pr[24 + warp] = t_af;
+            }
+        }
+    }
+
+    // ---- teardown
+    __syncthreads();
+    if (threadIdx.x == 0 && *s_abort) atomicOr(p.status, 1);
+    if (warp == kMmaWarp) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem_base, p.tmem_cols);
+    }
+}
+
+}  // namespace blamm

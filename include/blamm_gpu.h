@@ -151,6 +151,16 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
                        float *out);
 /* The guard band of each column in the current mode (ncols floats). */
 int blamm_guard_band(const blamm_ctx *ctx, float *out);
+/* Role timing of the tensor-core scan kernel: enable (1) / disable (0) it for
+ * later scans; read the last scan's counters (32 int64 per CTA, clock cycles:
+ * 0 MMA waits for a free accumulator, 1 MMA waits for E, 2 B-tile reloads,
+ * 3 MMA loop, 4 E-builder waits for a code window, 5 E-builder waits for a
+ * free E stage, 6 E-builder loop, 7 epilogue waits for an accumulator,
+ * 8 epilogue loop, 9 epilogue drain, 10 jobs, 11 E build, 12 epilogue rounds with
+ * candidates, 16-23 drain of epilogue warps 0-7, 24-31 their waits).  *nctas
+ * receives the CTA count. */
+int blamm_debug_profile(blamm_ctx *ctx, int enable);
+int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, int *nctas);
 
 #ifdef __cplusplus
 }
