@@ -76,11 +76,12 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_score_histograms.argtypes = [vp, vp, i64, vp, i64, vp, vp, C.c_int, vp]
     lib.blamm_debug_profile.argtypes = [vp, C.c_int]
     lib.blamm_debug_profile_read.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
+    lib.blamm_scan_device_static.argtypes = [vp, vp, i64, vp, i64, vp, i64, C.POINTER(i64)]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
                  "blamm_set_softmask", "blamm_score_histograms", "blamm_debug_profile",
-                 "blamm_debug_profile_read"):
+                 "blamm_debug_profile_read", "blamm_scan_device_static"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -162,6 +163,17 @@ class GpuScanner:
                                         C.c_void_p(d_hits), hit_cap, C.byref(nh))
         if rc == BLAMM_ERR_OVERFLOW:
             raise BlammError(rc, f"{nh.value} hits exceed the capacity {hit_cap}")
+        self._check(rc)
+        return nh.value
+
+    def scan_device_static(self, d_bases: int, n: int, d_runs: int, nruns: int, d_hits: int,
+                           hit_cap: int) -> int:
+        """scan_device through the allocation-free entry point (library-owned fixed scratch)."""
+        nh = C.c_int64(0)
+        rc = self.lib.blamm_scan_device_static(self.h, C.c_void_p(d_bases), n, C.c_void_p(d_runs), nruns,
+                                               C.c_void_p(d_hits), hit_cap, C.byref(nh))
+        if rc == BLAMM_ERR_OVERFLOW:
+            raise BlammError(rc, self.lib.blamm_last_error(self.h).decode())
         self._check(rc)
         return nh.value
 

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -913,6 +914,208 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
     }
     cudaFree(d_dump);
     return rc;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free scan
+//
+// blamm_scan_device_static keeps every per-call buffer of a scan (the packed
+// stream, the candidate list, the counters and the status word) in one
+// file-scope __device__ array instead of the context's cudaMalloc'd buffers,
+// so the call itself allocates no device or host memory.  The array is part of
+// this library's device image: each device gets its own copy when the module
+// is loaded there.  Its device address is looked up once per device with
+// cudaGetSymbolAddress (the host-side name of a __device__ array is not a
+// device address) with that device current.
+
+namespace {
+
+constexpr int64_t kStaticMaxBases = int64_t(8) << 20;  // positions per call
+constexpr int64_t kStaticWords32 = (kStaticMaxBases + kStreamPad + 31) / 32;
+constexpr int64_t kStaticCandCap = int64_t(2) << 20;   // tensor-core candidates per call
+constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kStaticSeq2Off = 0;
+constexpr size_t kStaticZmaskOff = round256(kStaticSeq2Off + sizeof(uint32_t) * 2 * kStaticWords32);
+constexpr size_t kStaticCandOff = round256(kStaticZmaskOff + sizeof(uint32_t) * kStaticWords32);
+constexpr size_t kStaticCountOff = round256(kStaticCandOff + sizeof(unsigned long long) * kStaticCandCap);
+constexpr size_t kStaticStatusOff = round256(kStaticCountOff + sizeof(unsigned long long) * 4);
+constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 19 MiB
+
+constexpr int kStaticMaxDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+static std::mutex g_static_mu;
+static unsigned char *g_static_ptr[kStaticMaxDevices] = {};
+
+// Device address of this device's scratch copy; the first call on a device
+// looks it up (the current device must be ctx->device).
+static int static_scratch(blamm_ctx *ctx, unsigned char **out)
+{
+    if (ctx->device < 0 || ctx->device >= kStaticMaxDevices)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "device %d: no static scratch slot", ctx->device);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[ctx->device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(ctx, BLAMM_ERR_CUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+        g_static_ptr[ctx->device] = static_cast<unsigned char *>(p);
+    }
+    *out = g_static_ptr[ctx->device];
+    return BLAMM_OK;
+}
+
+extern "C" {
+
+int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
+                             int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, int64_t *n_hits)
+{
+    if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
+    *n_hits = 0;
+    if (n > kStaticMaxBases)
+        return fail(ctx, BLAMM_ERR_ARG, "blamm_scan_device_static: %lld positions > the static limit %lld",
+                    (long long)n, (long long)kStaticMaxBases);
+    if (n == 0) return BLAMM_OK;
+    if (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits))
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    const bool tc = ctx->mode != BLAMM_MODE_FP32;
+    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    if (tc && !(ctx->plan_valid && ctx->plan_terms == terms))
+        return fail(ctx, BLAMM_ERR_STATE,
+                    "blamm_scan_device_static: no tensor-core plan for this bank, mode and thresholds "
+                    "(one blamm_scan or blamm_scan_device call builds it)");
+    CK(cudaSetDevice(ctx->device));
+    unsigned char *base = nullptr;
+    int rc = static_scratch(ctx, &base);
+    if (rc) return rc;
+    uint32_t *seq2 = reinterpret_cast<uint32_t *>(base + kStaticSeq2Off);
+    uint32_t *zmask = reinterpret_cast<uint32_t *>(base + kStaticZmaskOff);
+    unsigned long long *cand = reinterpret_cast<unsigned long long *>(base + kStaticCandOff);
+    unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + kStaticCountOff);
+    int *status = reinterpret_cast<int *>(base + kStaticStatusOff);
+
+    ctx->stats = blamm_stats{};
+    ctx->stats.positions = n;
+    ctx->stats.columns = ctx->ncols;
+    int launches = 0;
+    // the counters (candidates, hits) and the status word start at zero on every call
+    CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(status, 0, sizeof(int), ctx->stream));
+    const int64_t nwords32 = (n + kStreamPad + 31) / 32;
+    pack_kernel<<<(unsigned)((nwords32 + 255) / 256), 256, 0, ctx->stream>>>(d_bases, n, seq2, zmask, nwords32,
+                                                                          ctx->lower_scores);
+    CK(cudaGetLastError());
+    ++launches;
+
+    if (!tc) {
+        PlainParams p{};
+        p.seq2 = seq2;
+        p.zmask = zmask;
+        p.n = n;
+        p.run_start = d_run_start;
+        p.nruns = nruns;
+        p.P = ctx->d_P;
+        p.p_rows = ctx->p_rows;
+        p.ncols = ctx->ncols;
+        p.lmax = ctx->lmax;
+        p.col_len = ctx->d_len;
+        p.thr = ctx->d_thr;
+        p.hits = d_hits;
+        p.hit_count = counters + 1;
+        p.hit_cap = hit_cap;
+        const int threads = 256;
+        int cpb = 32;
+        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
+        p.cols_per_block = cpb;
+        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
+        const int64_t bx = (n + threads - 1) / threads;
+        const int by = (ctx->ncols + cpb - 1) / cpb;
+        if (by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
+        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
+        CK(cudaGetLastError());
+        ++launches;
+    } else {
+        const int64_t n_mtiles = (n + kBM - 1) / kBM;
+        const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+        const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
+        if ((int)L.total > ctx->max_smem)
+            return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
+        const uint32_t smem = std::max<uint32_t>(L.total, 116 * 1024);
+        TcParams p{};
+        p.seq2 = seq2;
+        p.zmask = zmask;
+        p.n = n;
+        p.n_mtiles = n_mtiles;
+        p.tiles = ctx->d_tiles;
+        p.ntiles = (int32_t)ctx->tiles.size();
+        p.terms = ctx->plan_terms;
+        p.bbuf = ctx->d_bbuf;
+        p.slot_col = ctx->d_slot_col;
+        p.erows = ctx->erows;
+        p.b_term_max = ctx->b_term_max;
+        p.tmem_cols = ctx->tmem_cols;
+        p.cand = cand;
+        p.cand_count = counters;
+        p.cand_cap = kStaticCandCap;
+        p.status = status;
+        p.wait_limit = ctx->wait_limit;
+        p.dump_ncols = ctx->ncols;
+        const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
+        scan_tc_kernel<false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+        CK(cudaGetLastError());
+        ++launches;
+        unsigned long long ncand = 0;
+        int st = 0;
+        CK(cudaMemcpyAsync(&ncand, counters, sizeof ncand, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(&st, status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (st) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
+        ctx->stats.candidates = (int64_t)ncand;
+        if ((int64_t)ncand > kStaticCandCap)
+            return fail(ctx, BLAMM_ERR_OVERFLOW,
+                        "blamm_scan_device_static: %llu candidates > the static limit %lld (scan fewer "
+                        "positions per call)", ncand, (long long)kStaticCandCap);
+        if (ncand > 0) {
+            RescoreParams r{};
+            r.cand = cand;
+            r.slot_col = ctx->d_slot_col;
+            r.cand_count = counters;
+            r.cand_cap = kStaticCandCap;
+            r.seq2 = seq2;
+            r.zmask = zmask;
+            r.n = n;
+            r.run_start = d_run_start;
+            r.nruns = nruns;
+            r.P = ctx->d_P;
+            r.p_rows = ctx->p_rows;
+            r.col_len = ctx->d_len;
+            r.thr = ctx->d_thr;
+            r.hits = d_hits;
+            r.hit_count = counters + 1;
+            r.hit_cap = hit_cap;
+            const int threads = 256;
+            const int64_t blocks = std::min<int64_t>(((int64_t)ncand + threads - 1) / threads,
+                                                     (int64_t)ctx->sm_count * 16);
+            rescore_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(r);
+            CK(cudaGetLastError());
+            ++launches;
+        }
+    }
+    unsigned long long nh = 0;
+    CK(cudaMemcpyAsync(&nh, counters + 1, sizeof nh, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stats.hits = (int64_t)nh;
+    ctx->stats.tiles = (int32_t)(tc ? ctx->tiles.size() : 0);
+    ctx->stats.launches = launches;
+    *n_hits = (int64_t)nh;
+    return (int64_t)nh > hit_cap ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld", (long long)nh,
+                                        (long long)hit_cap)
+                                 : BLAMM_OK;
 }
 
 }  // extern "C"

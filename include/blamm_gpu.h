@@ -162,6 +162,29 @@ int blamm_guard_band(const blamm_ctx *ctx, float *out);
 int blamm_debug_profile(blamm_ctx *ctx, int enable);
 int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, int *nctas);
 
+/* blamm_scan_device without allocation.  It has no counterpart in the
+ * reference; it is for callers that may not allocate device or host memory
+ * during a scan (a memory pool that must not grow, a host thread that must not
+ * block in the allocator).  Same arguments, results and status codes as
+ * blamm_scan_device, but the packed stream, candidate list, counters and
+ * status word live in one fixed array of device memory that this library
+ * declares (about 19 MiB per device, reserved when the library's device code
+ * is loaded there).  Limits: n <= 8 Mi positions per call (more gives
+ * BLAMM_ERR_ARG) and at most 2 Mi tensor-core candidates per call (more gives
+ * BLAMM_ERR_OVERFLOW: scan fewer positions per call).  The counters and the
+ * status word are set to zero at the start of every call.
+ * Preconditions: a bank (blamm_set_motifs) and, in the tensor-core modes, a
+ * plan for the current bank, mode and thresholds, which the first
+ * blamm_scan / blamm_scan_device after a change builds (otherwise
+ * BLAMM_ERR_STATE).  The first call on a device looks up the array's device
+ * address; make it before any stream capture.
+ * The array is shared by every context on a device: calls that overlap in
+ * time on one device (from two host threads, or on two streams) race on it
+ * and corrupt each other's results.  Serialise them. */
+int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n,
+                             const int64_t *d_run_start, int64_t nruns, blamm_hit *d_hits,
+                             int64_t hit_cap, int64_t *n_hits);
+
 #ifdef __cplusplus
 }
 #endif
