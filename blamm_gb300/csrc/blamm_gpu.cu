@@ -351,14 +351,16 @@ int blamm_ctx_create(int device, blamm_ctx **out)
         ctx->sm_count = prop.multiProcessorCount;
         ctx->max_smem = (int)prop.sharedMemPerBlockOptin;
         cudaFuncAttributes fa;
-        CK(cudaFuncGetAttributes(&fa, scan_tc_kernel<false>));  // fails if no sm_103a image fits
-        if (fa.maxThreadsPerBlock < kTcThreads)
-            return fail(ctx, BLAMM_ERR_UNSUPPORTED, "scan kernel: %d registers allow only %d threads per block (< %d)",
-                        fa.numRegs, fa.maxThreadsPerBlock, kTcThreads);
-        CK(cudaFuncSetAttribute(scan_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                ctx->max_smem));
-        CK(cudaFuncSetAttribute(scan_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                ctx->max_smem));
+        // fails if no sm_103a image fits
+        for (const void *k : {(const void *)scan_tc_kernel<false, false>, (const void *)scan_tc_kernel<true, false>,
+                              (const void *)scan_tc_kernel<false, true>}) {
+            CK(cudaFuncGetAttributes(&fa, k));
+            if (fa.maxThreadsPerBlock < kTcThreads)
+                return fail(ctx, BLAMM_ERR_UNSUPPORTED,
+                            "scan kernel: %d registers allow only %d threads per block (< %d)", fa.numRegs,
+                            fa.maxThreadsPerBlock, kTcThreads);
+            CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->max_smem));
+        }
         CK(cudaFuncSetAttribute(scan_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 ctx->max_smem));
         CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -533,8 +535,9 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
         if (njobs > 0) {
             CK(cudaEventRecord(ctx->ev[4], ctx->stream));
-            if (dump) scan_tc_kernel<true><<<grid, kTcThreads, smem, ctx->stream>>>(p);
-            else scan_tc_kernel<false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            if (dump) scan_tc_kernel<true, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            else if (p.prof) scan_tc_kernel<false, true><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            else scan_tc_kernel<false, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
             CK(cudaGetLastError());
             CK(cudaEventRecord(ctx->ev[5], ctx->stream));
             ++*launches;
@@ -1066,7 +1069,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.wait_limit = ctx->wait_limit;
         p.dump_ncols = ctx->ncols;
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-        scan_tc_kernel<false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+        scan_tc_kernel<false, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
         CK(cudaGetLastError());
         ++launches;
         unsigned long long ncand = 0;

@@ -129,6 +129,28 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
     return d;
 }
 
+// Named barrier over `count` threads (a multiple of 32).
+__device__ __forceinline__ void bar_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Named barrier over `count` threads that also returns whether any of them
+// passed pred = true.
+__device__ __forceinline__ bool bar_any(int id, int count, bool pred)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
 // Instruction descriptor for kind::f16 with BF16 A and B, FP32 accumulate,
 // both operands K-major, dense: D format bits 4-5 = 1 (F32), A format bits
 // 7-9 = 1 (BF16), B format bits 10-12 = 1 (BF16), N>>3 at bits 17-22,

@@ -27,9 +27,10 @@
 //
 // Roles (640 threads): warps 0-15 drain TMEM (lane quarter = warp % 4, column
 // group = warp / 4) and test sign bits; warp 16 allocates TMEM and one lane
-// issues the MMAs and the TMA bulk copies of B tiles; warp 17 builds E from
-// 2-bit code windows that it prefetches with TMA bulk copies kCodeStages jobs
-// ahead.  Two E stages and two TMEM accumulators keep the roles overlapped.
+// issues the MMAs and the TMA bulk copies of B tiles; warps 17-19 build E from
+// 2-bit code windows that one of their threads prefetches with TMA bulk copies
+// kCodeStages jobs ahead.  kEStages E stages and two TMEM accumulators keep the roles
+// overlapped.
 // Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
 // major, so a CTA reloads B only when its tile changes.  Every wait is
 // bounded: on a timeout the CTA raises an abort flag, every role stops,
@@ -47,8 +48,10 @@ constexpr int kMaxTcLen = 256;   // longest motif on the tensor-core path
 constexpr int kCandBuf = 128;    // per-warp staging of candidates in SMEM
 constexpr int kEpiWarps = 16;    // TMEM drain warps (4 per lane quarter)
 constexpr int kMmaWarp = 16;
-constexpr int kWWarp = 17;
-constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps); 18 and 19 idle
+constexpr int kWWarp = 17;      // first of the E-builder warps
+constexpr int kEWarps = 3;       // E-builder warps 17-19
+constexpr int kEBarrier = 1;     // named barrier of the E builders
+constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps)
 constexpr int kCodeStages = 4;   // code windows in flight
 constexpr int kEStages = 4;      // one-hot E stages
 
@@ -225,7 +228,17 @@ __device__ __forceinline__ int stage_candidates(uint32_t mask, int slot0, int64_
     return fill + total;
 }
 
-template <bool kDump>
+// Clock read for the role timing; compiled out (0) when kProf is false.
+template <bool kProf>
+__device__ __forceinline__ long long tick()
+{
+    if constexpr (kProf) return clock64();
+    else return 0;
+}
+
+// kDump: also write the raw accumulator of some positions (test hook);
+// kProf: role timing into p.prof.  The scan itself is <false, false>.
+template <bool kDump, bool kProf>
 __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
 {
     extern __shared__ uint8_t smem_raw[];
@@ -283,9 +296,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         // =========================== MMA issuer ===========================
         if (lane == 0) {
             int cur_tile = -1;
-            uint32_t bphase = 0, dphase = 0, idesc = 0, g_steps = 0, sbo_b = 0;
+            uint32_t bphase = 0, dphase = 0, idesc = 0, g_steps = 0;
+            uint64_t bdesc_hi0 = 0, bdesc_lo0 = 0;  // k-step 0 of the current tile's B terms
             long long t_acc = 0, t_w = 0, t_b = 0;
-            const long long t_start = clock64();
+            const long long t_start = tick<kProf>();
             const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
             uint32_t jc = 0;
             bool ok = true;
@@ -293,7 +307,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
                 const int tile = it.tile;
                 if (tile != cur_tile) {
-                    const long long tb = clock64();
+                    const long long tb = tick<kProf>();
                     if (cur_tile >= 0) {  // every MMA reading the old B must be done
                         ptx::mma_commit(bars + 8 * BAR_DRAIN);
                         ok = ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit);
@@ -311,35 +325,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     bphase ^= 1;
                     if (!ok) break;
                     cur_tile = tile;
-                    if (p.prof) t_b += clock64() - tb;
+                    if (kProf) t_b += tick<kProf>() - tb;
                     g_steps = (uint32_t)td.g;
                     idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
-                    sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
+                    const uint32_t sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
+                    bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
+                    bdesc_lo0 = ptx::smem_desc(sbase + L.b_lo, 128u, sbo_b);
                 }
                 const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;                   // accumulator
                 const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
-                const long long t0 = clock64();
+                const long long t0 = tick<kProf>();
                 ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
-                const long long t1 = clock64();
+                const long long t1 = tick<kProf>();
                 ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
-                if (p.prof) {
+                if (kProf) {
                     t_acc += t1 - t0;
-                    t_w += clock64() - t1;
+                    t_w += tick<kProf>() - t1;
                 }
                 if (!ok) break;
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem_base + s * acc_stride;
-                const uint32_t e_addr = sbase + L.e0 + es * (uint32_t)p.erows * 16u;
+                // A of k-step g starts 4g entries (64 B) into the E stage, B_g 256 B into each term:
+                // the descriptors' address fields (bits 0-13, in 16 B units) advance by 4 and 16
+                const uint64_t adesc0 = ptx::smem_desc(sbase + L.e0 + es * (uint32_t)p.erows * 16u, 32u, 128u);
                 // D = -T (bias pieces in the last k-step of the hi term)
-                ptx::mma_bf16(d_tmem, adesc_bias, ptx::smem_desc(sbase + L.b_hi + g_steps * 256u, 128u, sbo_b),
-                              idesc, 0u);
-                for (uint32_t g = 0; g < g_steps; ++g) {
-                    // A: entries 4g .. 4g+129 (rows 16 B apart, row groups 128 B, K cores 32 B)
-                    const uint64_t adesc = ptx::smem_desc(e_addr + 64u * g, 32u, 128u);
-                    ptx::mma_bf16(d_tmem, adesc, ptx::smem_desc(sbase + L.b_hi + g * 256u, 128u, sbo_b), idesc, 1u);
-                    if (p.terms == 2)
-                        ptx::mma_bf16(d_tmem, adesc, ptx::smem_desc(sbase + L.b_lo + g * 256u, 128u, sbo_b), idesc,
-                                      1u);
+                ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
+                if (p.terms == 2) {
+                    for (uint32_t g = 0; g < g_steps; ++g) {
+                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
+                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
+                    }
+                } else {
+                    for (uint32_t g = 0; g < g_steps; ++g)
+                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
                 }
                 ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
@@ -347,22 +365,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             // drain: nothing may still write TMEM when it is freed
             ptx::mma_commit(bars + 8 * BAR_DRAIN);
             if (!ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit)) *s_abort = 1;
-            if (p.prof) {
+            if (kProf) {
                 long long *pr = p.prof + 32 * blockIdx.x;
                 pr[0] = t_acc;
                 pr[1] = t_w;
                 pr[2] = t_b;
-                pr[3] = clock64() - t_start;
+                pr[3] = tick<kProf>() - t_start;
                 pr[10] = jc;
             }
         }
         __syncwarp();
-    } else if (warp == kWWarp) {
-        // ========================== E builder =============================
+    } else if (warp >= kWWarp) {
+        // ====================== E builders (warps 17-19) ======================
+        // Thread et = 0 (warp 17, lane 0) also prefetches the code windows.
+        const int et = threadIdx.x - kWWarp * 32;
         const uint32_t codes = sbase + L.codes;
         JobIter ahead;  // the job whose code window is fetched next
         ahead.init(blockIdx.x, p.n_mtiles);
-        auto fetch = [&](uint32_t jc) {  // lane 0: code window of the jc-th job into its ring stage
+        auto fetch = [&](uint32_t jc) {  // et 0: code window of the jc-th job into its ring stage
             if (ahead.job >= njobs) return;
             const int64_t m = ahead.m;
             ahead.next(gridDim.x, p.n_mtiles);
@@ -372,10 +392,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             ptx::bulk_g2s(dst, p.seq2 + m * (kBM / 16), seq_bytes, bars + 8 * (BAR_CODE + st));
             ptx::bulk_g2s(dst + seq_bytes, p.zmask + m * (kBM / 32), zm_bytes, bars + 8 * (BAR_CODE + st));
         };
-        if (lane == 0)
+        if (et == 0)
             for (uint32_t j = 0; j < kCodeStages; ++j) fetch(j);
         long long t_code = 0, t_we = 0, t_build = 0;
-        const long long t_start = clock64();
+        const long long t_start = tick<kProf>();
         uint32_t jc = 0;
         JobIter it;
         for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
@@ -384,13 +404,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const int entries = kBM + 4 * g + 2;
             const uint32_t cs = jc % kCodeStages, cph = (jc / kCodeStages) & 1u;
             const uint32_t s = jc % kEStages, ph = (jc / kEStages) & 1u;
-            const long long t0 = clock64();
-            if (!ptx::mbar_wait(bars + 8 * (BAR_CODE + cs), cph, s_abort, p.wait_limit)) break;
-            const long long t1 = clock64();
-            if (!ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit)) break;
-            if (p.prof) {
+            const long long t0 = tick<kProf>();
+            bool ok = ptx::mbar_wait(bars + 8 * (BAR_CODE + cs), cph, s_abort, p.wait_limit);
+            const long long t1 = tick<kProf>();
+            ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
+            // every builder thread leaves together when any of them gave up (no one is left
+            // waiting at the barrier below)
+            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok)) break;
+            if (kProf) {
                 t_code += t1 - t0;
-                t_we += clock64() - t1;
+                t_we += tick<kProf>() - t1;
             }
             const uint32_t *cw = reinterpret_cast<const uint32_t *>(smem + L.codes + cs * (seq_bytes + zm_bytes));
             const uint32_t *zw = cw + seq_bytes / 4;
@@ -401,32 +424,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 const uint32_t h = zero ? 0u : (0x3F80u << ((code & 1u) << 4));
                 return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
             };
-            const long long t2 = clock64();
-#pragma unroll 4
-            for (int i = lane; i < entries; i += 32) {
+            const long long t2 = tick<kProf>();
+#pragma unroll 2
+            for (int i = et; i < entries; i += kEWarps * 32) {
                 const int j = i + 1;
                 const uint2 a = onehot((cw[i >> 4] >> (2 * (i & 15))) & 3u, (zw[i >> 5] >> (i & 31)) & 1u);
                 const uint2 b = onehot((cw[j >> 4] >> (2 * (j & 15))) & 3u, (zw[j >> 5] >> (j & 31)) & 1u);
                 e[i] = make_uint4(a.x, a.y, b.x, b.y);
             }
-            __syncwarp();
-            if (p.prof) t_build += clock64() - t2;
-            if (lane == 0) {
-                ptx::fence_proxy_async_smem();  // the generic reads of stage cs precede its refill
+            // each writer makes its E entries visible to the tensor cores and orders its
+            // reads of code stage cs before the refill below
+            ptx::fence_proxy_async_smem();
+            ptx::bar_sync(kEBarrier, kEWarps * 32);
+            if (kProf) t_build += tick<kProf>() - t2;
+            if (et == 0) {
                 fetch(jc + kCodeStages);
+                ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
             }
-            ptx::fence_proxy_async_smem();  // E is read by the tensor cores
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
         }
-        if (p.prof && lane == 0) {
+        if (kProf && et == 0) {
             long long *pr = p.prof + 32 * blockIdx.x;
             pr[4] = t_code;
             pr[5] = t_we;
             pr[11] = t_build;
         }
         // a prefetched window may still be in flight when the loop ends early
-        if (lane == 0)
+        if (et == 0)
             for (uint32_t j = jc; j < jc + kCodeStages; ++j) {
                 const long long job = blockIdx.x + (long long)j * gridDim.x;
                 if (job >= njobs || *s_abort == 0) break;
@@ -440,7 +463,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         unsigned long long *buf = s_cand + warp * kCandBuf;
         int fill = 0;
         long long t_af = 0, t_dr = 0, n_rare = 0, t_ld = 0, t_f1 = 0, t_red = 0, t_f2 = 0;
-        const long long t_start = clock64();
+        const long long t_start = tick<kProf>();
         uint32_t jc = 0;
         JobIter it;
         for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
@@ -448,88 +471,81 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const int64_t m = it.m;
             const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
             const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;
-            const long long t0 = clock64();
+            const long long t0 = tick<kProf>();
             if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
-            const long long t1 = clock64();
-            if (p.prof) t_af += t1 - t0;
+            const long long t1 = tick<kProf>();
+            if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
-            if (p.prof) t_f1 += clock64() - t1;
+            if (kProf) t_f1 += tick<kProf>() - t1;
             const int64_t pos = m * kBM + q * 32 + lane;
             const bool valid = pos < p.n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + s * acc_stride;
-            const bool dump_row = kDump && pos >= p.dump_p0 && pos < p.dump_p0 + p.dump_npos;
-            // This warp's 32-column chunks grp and grp+4 (N <= 256) in one round of two
-            // TMEM loads, AND-reduced to one word whose sign bit is clear iff some column
-            // is a candidate, and only then (rare) turned into masks.  The accumulator is
-            // handed back after the reduction; staging comes after that.
-            uint32_t msk[2] = {0u, 0u};
-            bool anyw = false;
-#pragma unroll
-            for (int round = 0; round < 1; ++round) {
-                const int ca = grp, cb = grp + 4;
-                if (ca >= nch) break;  // warp-uniform
-                uint32_t va[32], vb[32];
-                const long long tl0 = clock64();
+            // This warp's 32-column chunks grp and grp+4 (N <= 256): two TMEM loads, after
+            // which the accumulator is handed back at once; the sign-bit test (an AND over
+            // the chunk: its sign bit is clear iff some column is a candidate), the rare
+            // mask building and the staging all run on the registers.
+            const int ca = grp, cb = grp + 4;
+            const bool has_a = ca < nch, has_b = cb < nch;  // warp-uniform
+            uint32_t va[32], vb[32];
+            const long long tl0 = tick<kProf>();
+            if (has_a) {
                 ptx::tmem_ld_32x32b_x32(taddr + ca * 32, va);
-                if (cb < nch) ptx::tmem_ld_32x32b_x32(taddr + cb * 32, vb);
+                if (has_b) ptx::tmem_ld_32x32b_x32(taddr + cb * 32, vb);
                 ptx::tmem_wait_ld();
                 ptx::reg_fence(va);
                 ptx::reg_fence(vb);
-                const long long tr0 = clock64();
-                const uint32_t r = cb < nch ? (and32(va) & and32(vb)) : and32(va);
+            }
+            const long long tf0 = tick<kProf>();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
+            if (kProf) {
+                const long long tf1 = tick<kProf>();
+                t_ld += tf0 - tl0;
+                t_f2 += tf1 - tf0;
+                t_dr += tf1 - t1;
+            }
+            if (has_a) {
+                const long long tr0 = tick<kProf>();
+                const uint32_t r = has_b ? (and32(va) & and32(vb)) : and32(va);
                 const bool any = valid && (int32_t)r >= 0;
-                if (__any_sync(0xffffffffu, any)) {
-                    anyw = true;
+                if (__any_sync(0xffffffffu, any)) {  // rare: stage this warp's candidates
+                    ++n_rare;
+                    uint32_t m0 = 0, m1 = 0;
                     if (any) {
-                        uint32_t m0 = 0, m1 = 0;
 #pragma unroll
                         for (int i = 0; i < 32; ++i) {
                             m0 |= ((~va[i]) >> 31) << i;
                             m1 |= ((~vb[i]) >> 31) << i;
                         }
-                        msk[0] = m0;
-                        msk[1] = cb < nch ? m1 : 0u;
+                        if (!has_b) m1 = 0u;
                     }
+                    fill = stage_candidates(m0, slot0 + ca * 32, pos, lane, buf, fill, p.cand, p.cand_count,
+                                            p.cand_cap);
+                    if (has_b)
+                        fill = stage_candidates(m1, slot0 + cb * 32, pos, lane, buf, fill, p.cand, p.cand_count,
+                                                p.cand_cap);
                 }
-                if (kDump && dump_row) {  // debug instantiation only: raw accumulator of some positions
+                if (kDump && pos >= p.dump_p0 && pos < p.dump_p0 + p.dump_npos) {
+                    // debug instantiation only: raw accumulator of some positions
                     float *row = p.dump + (pos - p.dump_p0) * p.dump_ncols;
 #pragma unroll
                     for (int i = 0; i < 32; ++i) {
                         int col = __ldg(p.slot_col + slot0 + ca * 32 + i);
                         if (col >= 0) row[col] = __uint_as_float(va[i]);
-                        if (cb < nch && (col = __ldg(p.slot_col + slot0 + cb * 32 + i)) >= 0)
+                        if (has_b && (col = __ldg(p.slot_col + slot0 + cb * 32 + i)) >= 0)
                             row[col] = __uint_as_float(vb[i]);
                     }
                 }
-                if (p.prof) {
-                    const long long tr1 = clock64();
-                    t_ld += tr0 - tl0;
-                    t_red += tr1 - tr0;
-                }
-            }
-            const long long tf0 = clock64();
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
-            if (p.prof) {
-                const long long tf1 = clock64();
-                t_f2 += tf1 - tf0;
-                t_dr += tf1 - t1;
-            }
-            if (anyw) {  // rare: stage this lane's candidates
-                ++n_rare;
-#pragma unroll
-                for (int k = 0; k < 2; ++k)
-                    fill = stage_candidates(msk[k], slot0 + (grp + 4 * k) * 32, pos, lane, buf, fill, p.cand,
-                                            p.cand_count, p.cand_cap);
+                if (kProf) t_red += tick<kProf>() - tr0;
             }
         }
         fill = flush_candidates(lane, buf, fill, p.cand, p.cand_count, p.cand_cap);
-        if (p.prof && lane == 0) {
+        if (kProf && lane == 0) {
             long long *pr = p.prof + 32 * blockIdx.x;
             if (warp == 0) {
                 pr[7] = t_af;
-                pr[8] = clock64() - t_start;
+                pr[8] = tick<kProf>() - t_start;
                 pr[9] = t_dr;
                 pr[12] = n_rare;
                 pr[13] = t_ld;
