@@ -46,6 +46,9 @@ def args_parse():
     ap.add_argument("--bases", type=int, default=100_000_000, help="total bases of the workload")
     ap.add_argument("--cpu-sample", type=int, default=8_000_000, help="bases in a CPU-baseline sample")
     ap.add_argument("--no-modes", action="store_true", help="skip the bf16 / fp32 comparison runs")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=48, help="distinct requests of the serving pool")
+    ap.add_argument("--serve-slots", type=int, default=8, help="requests in flight in the serving measurement")
     return ap.parse_args()
 
 
@@ -204,6 +207,74 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ serving (config 5)
+def run_serve(a) -> dict:
+    """Config-5 serving through the scan service (include/blamm_serve.h): a resident bank of
+    2000 motifs (4000 columns) with threshold sets for p = 1e-3, 1e-4, 1e-5; requests of
+    log-uniform 1 kbp-5 Mbp, U{1..2000} motifs, a random p.  First the saturation throughput
+    (every request queued at once), then Poisson arrivals at 25 / 50 / 90 % of it; latency =
+    submission to completion, measured by the service."""
+    from blamm_gb300 import Server, workloads
+    from blamm_gb300._native import MotifBank
+    pfms = workloads.config5_bank(a.seed)
+    bank = MotifBank.from_pfms([p for _, p in pfms], revcompl=True)
+    counts = np.array([2625, 2375, 2375, 2625], dtype=np.uint64)  # GC 0.475, the middle of the requests' range
+    bank.generate(counts, 0.25)
+    P, lens, _ = bank.matrix()
+    bgp = ((counts.astype(np.float32) + np.float32(0.25)) /
+           (np.float32(counts.sum()) + np.float32(1.0))).astype(np.float32)
+    sets = np.stack([bank.pvalue_thresholds(bgp, pv) for pv in workloads.CONFIG5_PVALUES])
+    reqs = workloads.config5_requests(a.seed, a.serve_requests)
+    req_cols = [np.stack([2 * m, 2 * m + 1], axis=1).ravel().astype(np.int32) for _, _, m, _ in reqs]
+    work = [len(b) * len(c) for (b, _, _, _), c in zip(reqs, req_cols)]
+    srv = Server(P, lens, sets, slots=a.serve_slots)
+    try:
+        for i in range(min(len(reqs), a.serve_slots)):  # warm-up: contexts, buffers, plans
+            srv.wait(srv.submit(reqs[i][0][:20_000], reqs[i][1], req_cols[i], reqs[i][3]))
+        # saturation: the whole pool queued at once
+        t0 = time.perf_counter()
+        ids = [srv.submit(b, r, c, st) for (b, r, _, st), c in zip(reqs, req_cols)]
+        lat = [srv.wait(i)[1] for i in ids]
+        wall = time.perf_counter() - t0
+        for i in ids:
+            srv.take(i)
+        sat_rate = len(reqs) / wall
+        out = {"workload": "config5: 2000 motifs (4000 columns), requests log-uniform 1 kbp-5 Mbp, "
+                           "U{1..2000} motifs, p in {1e-3, 1e-4, 1e-5}",
+               "slots": a.serve_slots, "pool": len(reqs),
+               "saturation": {"requests_per_s": sat_rate, "bp_motif_per_s": sum(work) / wall,
+                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
+               "open_loop": []}
+        rng = np.random.default_rng(a.seed + 77)
+        for load in (0.25, 0.5, 0.9):
+            rate = load * sat_rate
+            nreq = int(min(3 * len(reqs), max(len(reqs), rate * 6.0)))
+            gaps = rng.exponential(1.0 / rate, size=nreq)
+            order = rng.integers(0, len(reqs), size=nreq)
+            ids = []
+            t0 = time.perf_counter()
+            t_next = t0
+            for g, k in zip(gaps, order):
+                t_next += g
+                d = t_next - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                b, r, _, st = reqs[k]
+                ids.append(srv.submit(b, r, req_cols[k], st))
+            res = [srv.wait(i) for i in ids]
+            wall = time.perf_counter() - t0
+            for i in ids:
+                srv.take(i)
+            lat = [x[1] for x in res]
+            out["open_loop"].append({"load": load, "rate_req_s": rate, "requests": nreq,
+                                     "p50_ms": float(np.percentile(lat, 50)),
+                                     "p99_ms": float(np.percentile(lat, 99)),
+                                     "bp_motif_per_s": float(sum(work[k] for k in order)) / wall})
+        return out
+    finally:
+        srv.close()
+
+
 # ------------------------------------------------------------------ GPU side
 def run_ours(a, rank, world, local):
     import torch
@@ -345,6 +416,12 @@ def run_ours(a, rank, world, local):
         "modes": modes,
         "clocks": clk,
     }
+    if rank == 0 and world == 1 and not a.no_serve:
+        sc.close()
+        line["serve"] = run_serve(a)
+        if line["serve"]["open_loop"]:
+            line["serve_p50_ms"] = line["serve"]["open_loop"][-1]["p50_ms"]
+            line["serve_p99_ms"] = line["serve"]["open_loop"][-1]["p99_ms"]
     if rank == 0 and world == 1:
         v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -77,11 +77,27 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_debug_profile.argtypes = [vp, C.c_int]
     lib.blamm_debug_profile_read.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     lib.blamm_scan_device_static.argtypes = [vp, vp, i64, vp, i64, vp, i64, C.POINTER(i64)]
+    lib.blamm_set_columns.argtypes = [vp, vp, C.c_int]
+    lib.blamm_reserve.argtypes = [vp, i64, i64]
+    lib.blamm_scan_enqueue.argtypes = [vp, vp, i64, vp, i64, vp, i64, vp]
+    lib.blamm_scan_graph_create.argtypes = [vp, vp, i64, vp, i64, vp, i64, vp, C.POINTER(vp)]
+    lib.blamm_scan_graph_launch.argtypes = [vp, vp]
+    lib.blamm_scan_graph_destroy.argtypes = [vp]
+    lib.blamm_scan_graph_destroy.restype = None
+    lib.blamm_autotune.argtypes = [vp, vp, i64, vp, i64, C.POINTER(C.c_float)]
+    lib.blamm_theoretical_hist.argtypes = [vp, vp, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_uint64, C.c_int,
+                                           vp, C.c_int, vp, vp]
+    lib.blamm_device_memory.argtypes = [C.c_int, C.POINTER(i64), C.POINTER(i64)]
+    lib.blamm_set_plan_options.argtypes = [vp, C.c_int, C.c_float]
+    lib.blamm_get_plan_options.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
                  "blamm_set_softmask", "blamm_score_histograms", "blamm_debug_profile",
-                 "blamm_debug_profile_read", "blamm_scan_device_static"):
+                 "blamm_debug_profile_read", "blamm_scan_device_static", "blamm_set_columns",
+                 "blamm_reserve", "blamm_scan_enqueue", "blamm_scan_graph_create", "blamm_scan_graph_launch",
+                 "blamm_autotune", "blamm_theoretical_hist", "blamm_device_memory", "blamm_set_plan_options",
+                 "blamm_get_plan_options"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -177,6 +193,69 @@ class GpuScanner:
         self._check(rc)
         return nh.value
 
+    def set_columns(self, cols) -> None:
+        """Scan only these bank columns (None or empty: all)."""
+        if cols is None or len(cols) == 0:
+            self._check(self.lib.blamm_set_columns(self.h, None, 0))
+            return
+        c = np.ascontiguousarray(cols, dtype=np.int32)
+        self._check(self.lib.blamm_set_columns(self.h, _ptr(c), len(c)))
+
+    def reserve(self, max_positions: int, max_candidates: int) -> None:
+        self._check(self.lib.blamm_reserve(self.h, max_positions, max_candidates))
+
+    def enqueue(self, d_bases: int, n: int, d_runs: int, nruns: int, d_hits: int, hit_cap: int,
+                d_counts: int) -> None:
+        """Enqueue a scan without host synchronisation; counts land in d_counts (4 x uint64)."""
+        self._check(self.lib.blamm_scan_enqueue(self.h, C.c_void_p(d_bases), n, C.c_void_p(d_runs), nruns,
+                                                C.c_void_p(d_hits), hit_cap, C.c_void_p(d_counts)))
+
+    def graph_create(self, d_bases: int, n: int, d_runs: int, nruns: int, d_hits: int, hit_cap: int,
+                     d_counts: int) -> int:
+        g = C.c_void_p()
+        self._check(self.lib.blamm_scan_graph_create(self.h, C.c_void_p(d_bases), n, C.c_void_p(d_runs), nruns,
+                                                     C.c_void_p(d_hits), hit_cap, C.c_void_p(d_counts),
+                                                     C.byref(g)))
+        return g.value
+
+    def graph_launch(self, graph: int) -> None:
+        self._check(self.lib.blamm_scan_graph_launch(self.h, C.c_void_p(graph)))
+
+    def graph_destroy(self, graph: int) -> None:
+        self.lib.blamm_scan_graph_destroy(C.c_void_p(graph))
+
+    def theoretical_hist(self, P: np.ndarray, col_len: np.ndarray, bg_prob, pvalues=(), hist_of=None,
+                         nbins: int = 250, max_length: int = 10_000_000, fp64_dp: bool = False,
+                         counts: bool = False):
+        """GPU theoretical histograms: (thresholds (len(pvalues) x ncols), counts (ncols x nbins) or None)."""
+        Pc = np.ascontiguousarray(P, dtype=np.float32)
+        ln = np.ascontiguousarray(col_len, dtype=np.int32)
+        ncols, p_rows = Pc.shape
+        hof = None if hist_of is None else np.ascontiguousarray(hist_of, dtype=np.int32)
+        bg = np.ascontiguousarray(bg_prob, dtype=np.float32)
+        pv = np.ascontiguousarray(pvalues, dtype=np.float32)
+        thr = np.zeros((len(pv), ncols), dtype=np.float32)
+        cnt = np.zeros((ncols, nbins), dtype=np.uint64) if counts else None
+        self._check(self.lib.blamm_theoretical_hist(
+            self.h, _ptr(Pc), p_rows, ncols, _ptr(ln), _ptr(hof) if hof is not None else None, _ptr(bg), nbins,
+            max_length, int(fp64_dp), _ptr(pv) if len(pv) else None, len(pv), _ptr(thr) if len(pv) else None,
+            _ptr(cnt) if cnt is not None else None))
+        return thr, cnt
+
+    def set_plan_options(self, max_tile_columns: int, job_cost: float) -> None:
+        self._check(self.lib.blamm_set_plan_options(self.h, max_tile_columns, job_cost))
+
+    def plan_options(self) -> tuple[int, float]:
+        n, c = C.c_int(), C.c_float()
+        self._check(self.lib.blamm_get_plan_options(self.h, C.byref(n), C.byref(c)))
+        return n.value, c.value
+
+    def autotune(self, d_bases: int, n: int, d_runs: int, nruns: int) -> float:
+        ms = C.c_float(0.0)
+        self._check(self.lib.blamm_autotune(self.h, C.c_void_p(d_bases), n, C.c_void_p(d_runs), nruns,
+                                            C.byref(ms)))
+        return ms.value
+
     def stream(self) -> int:
         """The context's cudaStream_t as an integer handle."""
         p = C.c_void_p()
@@ -257,14 +336,107 @@ def host_lib() -> C.CDLL:
     lib.blamm_bank_matrix.argtypes = [vp, vp, vp, vp]
     lib.blamm_bank_min_max.argtypes = [vp, vp, vp]
     lib.blamm_bank_pvalue_thresholds.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, vp]
+    lib.blamm_bank_hist_columns.argtypes = [vp, vp]
+    lib.blamm_bank_hist_columns.restype = C.c_int
     lib.blamm_bank_name.argtypes = [vp, C.c_int]
     lib.blamm_bank_name.restype = C.c_char_p
     for name in ("blamm_bank_load", "blamm_bank_from_pfms", "blamm_bank_columns", "blamm_bank_max_len",
                  "blamm_bank_generate", "blamm_bank_matrix", "blamm_bank_min_max",
                  "blamm_bank_pvalue_thresholds"):
         getattr(lib, name).restype = C.c_int
+    i64 = C.c_int64
+    lib.blamm_server_create.argtypes = [C.POINTER(ServerConfig), vp, C.c_int, C.c_int, vp, vp, C.c_int,
+                                        C.POINTER(vp)]
+    lib.blamm_server_submit.argtypes = [vp, vp, i64, vp, i64, vp, C.c_int, C.c_int, C.POINTER(i64)]
+    lib.blamm_server_wait.argtypes = [vp, i64, i64, C.POINTER(i64), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
+    lib.blamm_server_take.argtypes = [vp, i64, vp, i64, C.POINTER(i64)]
+    lib.blamm_server_stats_get.argtypes = [vp, C.POINTER(ServerStats)]
+    lib.blamm_server_last_error.argtypes = [vp]
+    lib.blamm_server_last_error.restype = C.c_char_p
+    lib.blamm_server_destroy.argtypes = [vp]
+    lib.blamm_server_destroy.restype = None
+    for name in ("blamm_server_create", "blamm_server_submit", "blamm_server_wait", "blamm_server_take",
+                 "blamm_server_stats_get"):
+        getattr(lib, name).restype = C.c_int
     _host = lib
     return lib
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("mode", C.c_int), ("hbm_budget", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("queued", C.c_int64), ("bases", C.c_int64), ("bp_columns", C.c_double),
+                ("bytes_in_flight", C.c_int64), ("budget", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Server:
+    """The scan service of include/blamm_serve.h: resident bank + threshold sets, `slots`
+    requests in flight, admission by device memory."""
+
+    def __init__(self, P: np.ndarray, col_len: np.ndarray, thr_sets: np.ndarray, slots: int = 4,
+                 mode: str = "bf16x2", device: int = 0, hbm_budget: int = 0):
+        self.lib = host_lib()
+        Pc = np.ascontiguousarray(P, dtype=np.float32)  # (ncols, p_rows): column-major P
+        ln = np.ascontiguousarray(col_len, dtype=np.int32)
+        ts = np.ascontiguousarray(np.atleast_2d(thr_sets), dtype=np.float32)
+        cfg = ServerConfig(device, slots, MODES[mode], hbm_budget)
+        h = C.c_void_p()
+        rc = self.lib.blamm_server_create(C.byref(cfg), _ptr(Pc), Pc.shape[1], Pc.shape[0], _ptr(ln), _ptr(ts),
+                                          ts.shape[0], C.byref(h))
+        if rc != BLAMM_OK:
+            raise BlammError(rc, "cannot create the server")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.blamm_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int) -> None:
+        if rc != BLAMM_OK:
+            raise BlammError(rc, self.lib.blamm_server_last_error(self.h).decode())
+
+    def submit(self, bases, run_start, cols=None, thr_set: int = 0) -> int:
+        b = np.ascontiguousarray(np.frombuffer(bases, dtype=np.uint8)
+                                 if isinstance(bases, (bytes, bytearray)) else bases, dtype=np.uint8)
+        r = np.ascontiguousarray(run_start, dtype=np.int64)
+        c = None if cols is None or len(cols) == 0 else np.ascontiguousarray(cols, dtype=np.int32)
+        rid = C.c_int64()
+        self._check(self.lib.blamm_server_submit(self.h, _ptr(b), len(b), _ptr(r), len(r),
+                                                 _ptr(c) if c is not None else None, 0 if c is None else len(c),
+                                                 thr_set, C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> tuple[int, float, float]:
+        """(hits, latency ms, queueing ms) of a finished request."""
+        nh, lat, q = C.c_int64(), C.c_double(), C.c_double()
+        self._check(self.lib.blamm_server_wait(self.h, rid, timeout_ms, C.byref(nh), C.byref(lat), C.byref(q)))
+        return nh.value, lat.value, q.value
+
+    def take(self, rid: int) -> np.ndarray:
+        nh, _, _ = self.wait(rid)
+        out = np.empty(max(nh, 1), dtype=HIT_DTYPE)
+        n = C.c_int64()
+        self._check(self.lib.blamm_server_take(self.h, rid, out.ctypes.data_as(C.c_void_p), len(out), C.byref(n)))
+        return out[: n.value]
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self._check(self.lib.blamm_server_stats_get(self.h, C.byref(st)))
+        return st.as_dict()
 
 
 class MotifBank:
@@ -338,6 +510,13 @@ class MotifBank:
         if self.lib.blamm_bank_pvalue_thresholds(self.h, _ptr(bg), nbins, max_length, pvalue, _ptr(thr)) != 0:
             raise BlammError(-1, self.lib.blamm_host_last_error().decode())
         return thr
+
+    def hist_columns(self) -> np.ndarray:
+        """Per column, the forward column whose histogram gives its threshold."""
+        out = np.zeros(self.columns, dtype=np.int32)
+        if self.lib.blamm_bank_hist_columns(self.h, _ptr(out)) != 0:
+            raise BlammError(-1, self.lib.blamm_host_last_error().decode())
+        return out
 
     def name(self, c: int) -> str:
         return self.lib.blamm_bank_name(self.h, c).decode()

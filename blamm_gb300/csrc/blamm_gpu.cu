@@ -19,6 +19,7 @@
 #include "blamm_gpu.h"
 #include "scan_kernels.cuh"
 #include "scan_tc.cuh"
+#include "hist_kernels.cuh"
 
 using namespace blamm;
 
@@ -36,8 +37,12 @@ struct blamm_ctx {
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
 
-    // motif bank (host copy)
+    // motif bank (host copy); `active` lists the columns scanned (all when empty)
     int ncols = 0, p_rows = 0, lmax = 0;
+    std::vector<int32_t> active;
+    int32_t *d_active = nullptr;
+    size_t cap_active = 0;
+    bool active_dirty = false;
     std::vector<float> P;
     std::vector<int32_t> len;
     std::vector<float> thr;
@@ -53,9 +58,14 @@ struct blamm_ctx {
     std::vector<double> bias_T;  // per column: threshold - guard on the column grid
     int erows = 0;  // one-hot pair entries per E stage
     uint32_t b_term_max = 0, tmem_cols = 0;
+    int acc_stages = 2;
     TileDesc *d_tiles = nullptr;
     uint8_t *d_bbuf = nullptr;
     int32_t *d_slot_col = nullptr;
+    size_t cap_tiles = 0, cap_bbuf = 0, cap_slot_col = 0;
+    // planner knobs (the autotuner sets them): widest N tile, fixed cycles per job
+    int plan_nmax = 256;
+    double plan_job_cost = 200.0;
 
     // stream buffers
     char *d_bases = nullptr;
@@ -98,17 +108,25 @@ static int fail(blamm_ctx *c, int code, const char *fmt, ...)
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
+// Grow a context buffer to at least `need` elements.  The stream-ordered
+// allocator keeps a growing buffer from synchronising the whole device (other
+// contexts' work keeps running); every use of these buffers is on ctx->stream.
 template <typename T>
 static int ensure(blamm_ctx *ctx, T **ptr, size_t *cap, size_t need)
 {
     if (need <= *cap && *ptr) return BLAMM_OK;
-    if (*ptr) cudaFree(*ptr);
+    if (*ptr) CK(cudaFreeAsync(*ptr, ctx->stream));
     *ptr = nullptr;
     *cap = 0;
     size_t n = std::max<size_t>(need, 1);
-    CK(cudaMalloc((void **)ptr, n * sizeof(T)));
+    CK(cudaMallocAsync((void **)ptr, n * sizeof(T), ctx->stream));
     *cap = n;
     return BLAMM_OK;
+}
+
+static int scanned_columns(const blamm_ctx *ctx)
+{
+    return ctx->active.empty() ? ctx->ncols : (int)ctx->active.size();
 }
 
 // ------------------------------------------------------------------ planning
@@ -149,50 +167,56 @@ inline uint16_t bf16_bits_exact(double v)
 
 static int build_plan(blamm_ctx *ctx, int terms)
 {
-    const int ncols = ctx->ncols;
-    if (ctx->lmax > kMaxTcLen)
+    // the scanned columns, sorted by length (the reference's order already is, fwd/rc interleaved)
+    std::vector<int> order;
+    if (ctx->active.empty()) {
+        order.resize(ctx->ncols);
+        for (int i = 0; i < ctx->ncols; ++i) order[i] = i;
+    } else {
+        order.assign(ctx->active.begin(), ctx->active.end());
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ctx->len[a] < ctx->len[b]; });
+    const int nsel = (int)order.size();
+    const int lmax_sel = nsel ? ctx->len[order.back()] : 1;
+    if (lmax_sel > kMaxTcLen)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED,
-                    "motif length %d exceeds the tensor-core limit %d (use BLAMM_MODE_FP32)",
-                    ctx->lmax, kMaxTcLen);
-    // columns sorted by length (the reference's order already is, fwd/rc interleaved)
-    std::vector<int> order(ncols);
-    for (int i = 0; i < ncols; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return ctx->len[a] < ctx->len[b]; });
+                    "motif length %d exceeds the tensor-core limit %d (use BLAMM_MODE_FP32)", lmax_sel,
+                    kMaxTcLen);
 
-    const int gmax_all = std::max(1, (ctx->lmax + 3) / 4);
+    const int gmax_all = std::max(1, (lmax_sel + 3) / 4);
     const int erows_all = kBM + 4 * gmax_all + 8;
     const long long smem_limit = (long long)ctx->max_smem;
-    // everything but the B tiles (W stages, bias A tile, candidate staging, ...)
+    // everything but the B tiles (E stages, bias A tile, code ring, candidate staging, ...)
     const long long other = (long long)kEStages * erows_all * 16 + 4096 +
                             (long long)kCodeStages * (code_seq_bytes(erows_all) + code_zm_bytes(erows_all)) +
                             (long long)kEpiWarps * kCandBuf * 8 + 256LL * sizeof(TileDesc) + 64 + 128 + 64 + 2048 +
                             1024;
     const long long b_term_cap = (smem_limit - other) / terms;
+    const int ncap = std::max(32, std::min(256, ctx->plan_nmax / 32 * 32));
     // widest tile whose B terms (g motif k-steps + 1 bias k-step) fit shared memory
     auto nmax_for = [&](int g) {
         long long n = b_term_cap / (32LL * (g + 1));
         n = n / 32 * 32;
-        return (int)std::min<long long>(256, n);
+        return (int)std::min<long long>(ncap, n);
     };
     if (nmax_for(gmax_all) < 32)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "motif bank does not fit shared memory");
 
     // DP over sorted columns: tile = contiguous run of sorted columns.
-    // Per-job cycle model: MMA = (terms*g + 1)*N/2 (bias step included),
-    // epilogue ~ N (8 warps, sign tests), W build ~ 300, fixed overhead ~ 200.
+    // Per-job cycle model: MMA = (terms*g + 1)*N/2 (bias step included), epilogue ~ N,
+    // plus a fixed cost per job (E build, hand-offs).
     const double kInf = 1e300;
-    std::vector<double> f(ncols + 1, kInf);
-    std::vector<int> from(ncols + 1, -1);
+    std::vector<double> f(nsel + 1, kInf);
+    std::vector<int> from(nsel + 1, -1);
     f[0] = 0.0;
-    for (int j = 1; j <= ncols; ++j) {
+    for (int j = 1; j <= nsel; ++j) {
         for (int i = j - 1; i >= 0 && j - i <= 256; --i) {
             const int L = ctx->len[order[j - 1]];
             const int g = std::max(1, (L + 3) / 4);
             const int N = (j - i + 31) / 32 * 32;
             if (N > nmax_for(g)) break;
             const double mma = (terms * g + 1) * N / 2.0, epi = 1.0 * N;
-            const double cost = std::max(std::max(mma, epi), 300.0) + 200.0;
+            const double cost = std::max(std::max(mma, epi), 300.0) + ctx->plan_job_cost;
             if (f[i] + cost < f[j]) {
                 f[j] = f[i] + cost;
                 from[j] = i;
@@ -201,14 +225,15 @@ static int build_plan(blamm_ctx *ctx, int terms)
         if (from[j] < 0) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "tile planning failed");
     }
     std::vector<std::pair<int, int>> spans;
-    for (int j = ncols; j > 0; j = from[j]) spans.push_back({from[j], j});
+    for (int j = nsel; j > 0; j = from[j]) spans.push_back({from[j], j});
     std::reverse(spans.begin(), spans.end());
+    const int ncols = ctx->ncols;
 
-    // per-column quantisation and guard band
-    std::vector<int> kcol(ncols);
+    // per-column quantisation and guard band (scanned columns only)
+    std::vector<int> kcol(ncols, 0);
     ctx->guard.assign(ncols, 0.0f);
     std::vector<double> guard_d(ncols, 0.0);
-    for (int c = 0; c < ncols; ++c) {
+    for (const int c : order) {
         const float *col = &ctx->P[(size_t)c * ctx->p_rows];
         const int L = ctx->len[c];
         const int k = 7 - column_exponent(col, L);
@@ -301,23 +326,22 @@ static int build_plan(blamm_ctx *ctx, int terms)
         nmax = std::max(nmax, N);
     }
 
-    // upload
-    if (ctx->d_tiles) cudaFree(ctx->d_tiles);
-    if (ctx->d_bbuf) cudaFree(ctx->d_bbuf);
-    if (ctx->d_slot_col) cudaFree(ctx->d_slot_col);
-    ctx->d_tiles = nullptr;
-    ctx->d_bbuf = nullptr;
-    ctx->d_slot_col = nullptr;
-    CK(cudaMalloc(&ctx->d_tiles, sizeof(TileDesc) * tiles.size()));
-    CK(cudaMalloc(&ctx->d_bbuf, bbuf.size()));
-    CK(cudaMalloc(&ctx->d_slot_col, sizeof(int32_t) * slot_col.size()));
-    CK(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_bbuf, bbuf.data(), bbuf.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_slot_col, slot_col.data(), sizeof(int32_t) * slot_col.size(), cudaMemcpyHostToDevice));
+    // upload (buffers are reused; the copies are ordered on the context's stream)
+    int rc = ensure(ctx, &ctx->d_tiles, &ctx->cap_tiles, tiles.size());
+    if (!rc) rc = ensure(ctx, &ctx->d_bbuf, &ctx->cap_bbuf, bbuf.size());
+    if (!rc) rc = ensure(ctx, &ctx->d_slot_col, &ctx->cap_slot_col, slot_col.size());
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_tiles, tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_bbuf, bbuf.data(), bbuf.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_slot_col, slot_col.data(), sizeof(int32_t) * slot_col.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
     ctx->tiles = tiles;
     ctx->erows = kBM + 4 * gmax + 8;
     ctx->b_term_max = btmax;
-    ctx->tmem_cols = nmax <= 128 ? 256u : 512u;
+    ctx->tmem_cols = 512u;  // the whole TMEM: 4 accumulators of <= 128 columns or 2 of <= 256
+    ctx->acc_stages = nmax <= 128 ? 4 : 2;
     ctx->plan_terms = terms;
     ctx->plan_valid = true;
     return BLAMM_OK;
@@ -386,7 +410,8 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     void *bufs[] = {ctx->d_P,      ctx->d_len,   ctx->d_thr,      ctx->d_tiles, ctx->d_bbuf,
                     ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask,
-                    ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status};
+                    ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status,
+                    ctx->d_active};
     for (void *b : bufs)
         if (b) cudaFree(b);
     for (auto &ev : ctx->ev)
@@ -418,6 +443,8 @@ int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols, cons
         if (col_len[c] <= 0 || 4 * col_len[c] > p_rows)
             return fail(ctx, BLAMM_ERR_ARG, "column %d: length %d does not fit %d rows", c, col_len[c],
                         p_rows);
+        if (col_len[c] > kMaxMotifLen)
+            return fail(ctx, BLAMM_ERR_UNSUPPORTED, "column %d: length %d > %d", c, col_len[c], kMaxMotifLen);
         lmax = std::max(lmax, (int)col_len[c]);
     }
     CK(cudaSetDevice(ctx->device));
@@ -427,6 +454,7 @@ int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols, cons
     ctx->P.assign(P, P + (size_t)p_rows * ncols);
     ctx->len.assign(col_len, col_len + ncols);
     ctx->thr.assign(thr, thr + ncols);
+    ctx->active.clear();
     if (ctx->d_P) cudaFree(ctx->d_P);
     if (ctx->d_len) cudaFree(ctx->d_len);
     if (ctx->d_thr) cudaFree(ctx->d_thr);
@@ -439,6 +467,36 @@ int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols, cons
     CK(cudaMemcpy(ctx->d_P, ctx->P.data(), sizeof(float) * ctx->P.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_len, ctx->len.data(), sizeof(int32_t) * ncols, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_thr, ctx->thr.data(), sizeof(float) * ncols, cudaMemcpyHostToDevice));
+    ctx->plan_valid = false;
+    return BLAMM_OK;
+}
+
+int blamm_set_columns(blamm_ctx *ctx, const int32_t *cols, int n)
+{
+    if (!ctx || n < 0 || (n > 0 && !cols)) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    if (n > ctx->ncols) return fail(ctx, BLAMM_ERR_ARG, "%d columns > bank size %d", n, ctx->ncols);
+    std::vector<int32_t> act;
+    if (n > 0) {
+        std::vector<char> seen(ctx->ncols, 0);
+        act.reserve(n);
+        for (int i = 0; i < n; ++i) {
+            const int c = cols[i];
+            if (c < 0 || c >= ctx->ncols) return fail(ctx, BLAMM_ERR_ARG, "column %d is not in the bank", c);
+            if (seen[c]) return fail(ctx, BLAMM_ERR_ARG, "column %d is listed twice", c);
+            seen[c] = 1;
+            act.push_back(c);
+        }
+    }
+    CK(cudaSetDevice(ctx->device));
+    ctx->active.swap(act);
+    if (!ctx->active.empty()) {
+        int rc = ensure(ctx, &ctx->d_active, &ctx->cap_active, ctx->active.size());
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(ctx->d_active, ctx->active.data(), sizeof(int32_t) * ctx->active.size(),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
     ctx->plan_valid = false;
     return BLAMM_OK;
 }
@@ -517,6 +575,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         p.erows = ctx->erows;
         p.b_term_max = ctx->b_term_max;
         p.tmem_cols = ctx->tmem_cols;
+        p.acc_stages = ctx->acc_stages;
         p.cand = ctx->d_cand;
         p.cand_count = ctx->d_counters;
         p.cand_cap = ctx->cand_cap;
@@ -558,7 +617,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         if ((int64_t)ncand <= ctx->cand_cap) break;
         // grow and re-run
         size_t cap = 0;
-        cudaFree(ctx->d_cand);
+        CK(cudaFreeAsync(ctx->d_cand, ctx->stream));
         ctx->d_cand = nullptr;
         ctx->cand_cap = 0;
         rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)(ncand + ncand / 4 + 1024));
@@ -609,10 +668,11 @@ static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t n
     p.nruns = nruns;
     p.P = ctx->d_P;
     p.p_rows = ctx->p_rows;
-    p.ncols = ctx->ncols;
+    p.ncols = scanned_columns(ctx);
     p.lmax = ctx->lmax;
     p.col_len = ctx->d_len;
     p.thr = ctx->d_thr;
+    p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
     p.hits = d_hits;
     p.hit_count = ctx->d_counters + 1;
     p.hit_cap = hit_cap;
@@ -622,7 +682,7 @@ static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t n
     p.cols_per_block = cpb;
     const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
     const int64_t bx = (n + threads - 1) / threads;
-    const int by = (ctx->ncols + cpb - 1) / cpb;
+    const int by = (p.ncols + cpb - 1) / cpb;
     if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
     if (bx > 0) {
         CK(cudaEventRecord(ctx->ev[4], ctx->stream));
@@ -643,7 +703,7 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     ctx->stats = blamm_stats{};
     ctx->plain_timed = ctx->rescore_timed = false;
     ctx->stats.positions = n;
-    ctx->stats.columns = ctx->ncols;
+    ctx->stats.columns = scanned_columns(ctx);
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     int rc = launch_pack(ctx, d_bases, n);
     if (rc) return rc;
@@ -748,6 +808,22 @@ int blamm_device_count(int *n)
         return BLAMM_OK;
     }
     *n = c;
+    return BLAMM_OK;
+}
+
+int blamm_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes)
+{
+    if (!free_bytes || !total_bytes) return BLAMM_ERR_ARG;
+    *free_bytes = *total_bytes = 0;
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return BLAMM_ERR_CUDA;
+    if (cudaSetDevice(device) != cudaSuccess) return BLAMM_ERR_CUDA;
+    size_t f = 0, t = 0;
+    const cudaError_t e = cudaMemGetInfo(&f, &t);
+    cudaSetDevice(cur);
+    if (e != cudaSuccess) return BLAMM_ERR_CUDA;
+    *free_bytes = (int64_t)f;
+    *total_bytes = (int64_t)t;
     return BLAMM_OK;
 }
 
@@ -1004,7 +1080,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
 
     ctx->stats = blamm_stats{};
     ctx->stats.positions = n;
-    ctx->stats.columns = ctx->ncols;
+    ctx->stats.columns = scanned_columns(ctx);
     int launches = 0;
     // the counters (candidates, hits) and the status word start at zero on every call
     CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
@@ -1024,10 +1100,11 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.nruns = nruns;
         p.P = ctx->d_P;
         p.p_rows = ctx->p_rows;
-        p.ncols = ctx->ncols;
+        p.ncols = scanned_columns(ctx);
         p.lmax = ctx->lmax;
         p.col_len = ctx->d_len;
         p.thr = ctx->d_thr;
+        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
         p.hits = d_hits;
         p.hit_count = counters + 1;
         p.hit_cap = hit_cap;
@@ -1037,7 +1114,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.cols_per_block = cpb;
         const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
         const int64_t bx = (n + threads - 1) / threads;
-        const int by = (ctx->ncols + cpb - 1) / cpb;
+        const int by = (p.ncols + cpb - 1) / cpb;
         if (by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
         scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
         CK(cudaGetLastError());
@@ -1062,6 +1139,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.erows = ctx->erows;
         p.b_term_max = ctx->b_term_max;
         p.tmem_cols = ctx->tmem_cols;
+        p.acc_stages = ctx->acc_stages;
         p.cand = cand;
         p.cand_count = counters;
         p.cand_cap = kStaticCandCap;
@@ -1119,6 +1197,332 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
     return (int64_t)nh > hit_cap ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld", (long long)nh,
                                         (long long)hit_cap)
                                  : BLAMM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ enqueued scans, graphs, autotuning
+
+extern "C" {
+
+int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
+{
+    if (!ctx || max_positions < 0 || max_candidates < 0) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    CK(cudaSetDevice(ctx->device));
+    const int64_t nwords32 = (max_positions + kStreamPad + 31) / 32;
+    int rc = ensure(ctx, &ctx->d_seq2, &ctx->cap_words32, (size_t)(2 * nwords32));
+    if (!rc) rc = ensure(ctx, &ctx->d_zmask, &ctx->cap_zmask, (size_t)nwords32);
+    if (rc) return rc;
+    if (ctx->mode != BLAMM_MODE_FP32) {
+        if ((rc = ensure_plan(ctx))) return rc;
+        if (max_candidates > ctx->cand_cap) {
+            size_t cap = ctx->cand_cap > 0 ? (size_t)ctx->cand_cap : 0;
+            rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)max_candidates);
+            if (rc) return rc;
+            ctx->cand_cap = (int64_t)cap;
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BLAMM_OK;
+}
+
+int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start, int64_t nruns,
+                       blamm_hit *d_hits, int64_t hit_cap, uint64_t *d_counts)
+{
+    if (!ctx || !d_counts || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    const int64_t nwords32 = (n + kStreamPad + 31) / 32;
+    if ((size_t)(2 * nwords32) > ctx->cap_words32 || (size_t)nwords32 > ctx->cap_zmask)
+        return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: %lld positions exceed the reservation",
+                    (long long)n);
+    const bool tc = ctx->mode != BLAMM_MODE_FP32;
+    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    if (tc && (!(ctx->plan_valid && ctx->plan_terms == terms) || ctx->cand_cap <= 0))
+        return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: call blamm_reserve after changing the bank, "
+                                          "columns, thresholds or mode");
+    if (n > 0 && (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits)))
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemsetAsync(d_counts, 0, 4 * sizeof(uint64_t), ctx->stream));
+    if (n == 0) return BLAMM_OK;
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(d_counts);
+    pack_kernel<<<(unsigned)((nwords32 + 255) / 256), 256, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
+                                                                          nwords32, ctx->lower_scores);
+    CK(cudaGetLastError());
+    if (!tc) {
+        PlainParams p{};
+        p.seq2 = ctx->d_seq2;
+        p.zmask = ctx->d_zmask;
+        p.n = n;
+        p.run_start = d_run_start;
+        p.nruns = nruns;
+        p.P = ctx->d_P;
+        p.p_rows = ctx->p_rows;
+        p.ncols = scanned_columns(ctx);
+        p.lmax = ctx->lmax;
+        p.col_len = ctx->d_len;
+        p.thr = ctx->d_thr;
+        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
+        p.hits = d_hits;
+        p.hit_count = cnt + 1;
+        p.hit_cap = hit_cap;
+        const int threads = 256;
+        int cpb = 32;
+        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
+        p.cols_per_block = cpb;
+        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
+        const int64_t bx = (n + threads - 1) / threads;
+        const int by = (p.ncols + cpb - 1) / cpb;
+        if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
+        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
+        CK(cudaGetLastError());
+        return BLAMM_OK;
+    }
+    const int64_t n_mtiles = (n + kBM - 1) / kBM;
+    const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
+    if ((int)L.total > ctx->max_smem)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
+    TcParams p{};
+    p.seq2 = ctx->d_seq2;
+    p.zmask = ctx->d_zmask;
+    p.n = n;
+    p.n_mtiles = n_mtiles;
+    p.tiles = ctx->d_tiles;
+    p.ntiles = (int32_t)ctx->tiles.size();
+    p.terms = ctx->plan_terms;
+    p.bbuf = ctx->d_bbuf;
+    p.slot_col = ctx->d_slot_col;
+    p.erows = ctx->erows;
+    p.b_term_max = ctx->b_term_max;
+    p.tmem_cols = ctx->tmem_cols;
+    p.acc_stages = ctx->acc_stages;
+    p.cand = ctx->d_cand;
+    p.cand_count = cnt;
+    p.cand_cap = ctx->cand_cap;
+    p.status = reinterpret_cast<int *>(cnt + 2);
+    p.wait_limit = ctx->wait_limit;
+    p.dump_ncols = ctx->ncols;
+    const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
+    scan_tc_kernel<false, false><<<grid, kTcThreads, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream>>>(p);
+    CK(cudaGetLastError());
+    RescoreParams r{};
+    r.cand = ctx->d_cand;
+    r.slot_col = ctx->d_slot_col;
+    r.cand_count = cnt;
+    r.cand_cap = ctx->cand_cap;
+    r.seq2 = ctx->d_seq2;
+    r.zmask = ctx->d_zmask;
+    r.n = n;
+    r.run_start = d_run_start;
+    r.nruns = nruns;
+    r.P = ctx->d_P;
+    r.p_rows = ctx->p_rows;
+    r.col_len = ctx->d_len;
+    r.thr = ctx->d_thr;
+    r.hits = d_hits;
+    r.hit_count = cnt + 1;
+    r.hit_cap = hit_cap;
+    // a fixed grid: the candidate count is only known on the device
+    rescore_kernel<<<(unsigned)(ctx->sm_count * 8), 256, 0, ctx->stream>>>(r);
+    CK(cudaGetLastError());
+    return BLAMM_OK;
+}
+
+int blamm_scan_graph_create(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
+                            int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, uint64_t *d_counts, void **graph)
+{
+    if (!ctx || !graph) return BLAMM_ERR_ARG;
+    *graph = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = blamm_scan_enqueue(ctx, d_bases, n, d_run_start, nruns, d_hits, hit_cap, d_counts);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t e2 = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e2));
+    *graph = ge;
+    return BLAMM_OK;
+}
+
+int blamm_scan_graph_launch(blamm_ctx *ctx, void *graph)
+{
+    if (!ctx || !graph) return BLAMM_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph), ctx->stream));
+    return BLAMM_OK;
+}
+
+void blamm_scan_graph_destroy(void *graph)
+{
+    if (graph) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph));
+}
+
+int blamm_set_plan_options(blamm_ctx *ctx, int max_tile_columns, float job_cost)
+{
+    if (!ctx || max_tile_columns < 32 || max_tile_columns > 256 || !(job_cost >= 0.0f)) return BLAMM_ERR_ARG;
+    ctx->plan_nmax = max_tile_columns;
+    ctx->plan_job_cost = job_cost;
+    ctx->plan_valid = false;
+    return BLAMM_OK;
+}
+
+int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *job_cost)
+{
+    if (!ctx || !max_tile_columns || !job_cost) return BLAMM_ERR_ARG;
+    *max_tile_columns = ctx->plan_nmax;
+    *job_cost = (float)ctx->plan_job_cost;
+    return BLAMM_OK;
+}
+
+int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start, int64_t nruns,
+                   float *best_ms)
+{
+    if (!ctx || n < 0) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    if (best_ms) *best_ms = 0.0f;
+    if (ctx->mode == BLAMM_MODE_FP32 || n == 0) return BLAMM_OK;
+    if (!d_bases || !d_run_start || nruns <= 0) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    // a sample of up to 16 Mi positions (the runs that start inside it)
+    const int64_t ns = std::min<int64_t>(n, int64_t(16) << 20);
+    std::vector<int64_t> runs((size_t)nruns);
+    CK(cudaMemcpy(runs.data(), d_run_start, sizeof(int64_t) * nruns, cudaMemcpyDeviceToHost));
+    const int64_t nrs = std::max<int64_t>(1, std::lower_bound(runs.begin(), runs.end(), ns) - runs.begin());
+    size_t hc = (size_t)ctx->hits_cap;
+    int rc = ensure(ctx, &ctx->d_hits, &hc, (size_t)1 << 20);
+    if (rc) return rc;
+    ctx->hits_cap = (int64_t)hc;
+    const int nmax_opts[] = {128, 192, 256};
+    const double cost_opts[] = {200.0, 700.0, 1500.0};
+    const int keep_nmax = ctx->plan_nmax;
+    const double keep_cost = ctx->plan_job_cost;
+    float best = std::numeric_limits<float>::infinity();
+    int bn = keep_nmax;
+    double bc = keep_cost;
+    for (int nm : nmax_opts)
+        for (double jc : cost_opts) {
+            ctx->plan_nmax = nm;
+            ctx->plan_job_cost = jc;
+            ctx->plan_valid = false;
+            float t[3];
+            for (int rep = 0; rep < 3; ++rep) {
+                int64_t nh = 0;
+                rc = scan_core(ctx, d_bases, ns, d_run_start, nrs, ctx->d_hits, ctx->hits_cap, &nh);
+                if (rc && rc != BLAMM_ERR_OVERFLOW) {
+                    ctx->plan_nmax = keep_nmax;
+                    ctx->plan_job_cost = keep_cost;
+                    ctx->plan_valid = false;
+                    return rc;
+                }
+                t[rep] = ctx->stats.scan_ms;
+            }
+            std::sort(t, t + 3);
+            if (t[1] < best) {
+                best = t[1];
+                bn = nm;
+                bc = jc;
+            }
+        }
+    ctx->plan_nmax = bn;
+    ctx->plan_job_cost = bc;
+    ctx->plan_valid = false;
+    if ((rc = ensure_plan(ctx))) return rc;
+    if (best_ms) *best_ms = best;
+    return BLAMM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ theoretical histograms, thresholds
+
+extern "C" {
+
+int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols, const int32_t *col_len,
+                           const int32_t *hist_of, const float bg_prob[4], int nbins, uint64_t max_length,
+                           int fp64_dp, const float *pvalues, int npv, float *thr, uint64_t *counts)
+{
+    if (!ctx || !P || !col_len || !bg_prob || ncols <= 0 || p_rows <= 0 || nbins < 1 || nbins > 4096 ||
+        npv < 0 || (npv > 0 && (!pvalues || !thr)))
+        return BLAMM_ERR_ARG;
+    for (int c = 0; c < ncols; ++c) {
+        const int h = hist_of ? hist_of[c] : c;
+        if (h < 0 || h >= ncols) return fail(ctx, BLAMM_ERR_ARG, "hist_of[%d] = %d is not a column", c, h);
+        if (col_len[h] <= 0 || col_len[h] > kMaxMotifLen || 4 * col_len[h] > p_rows)
+            return fail(ctx, BLAMM_ERR_ARG, "column %d: bad length %d", h, col_len[h]);
+    }
+    CK(cudaSetDevice(ctx->device));
+    const int kmax = 8192;
+    const size_t smem = theo_smem_bytes(kmax, nbins, fp64_dp);
+    if (smem > (size_t)ctx->max_smem) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "histogram does not fit");
+    std::vector<int32_t> hof(ncols);
+    for (int c = 0; c < ncols; ++c) hof[c] = hist_of ? hist_of[c] : c;
+    float *d_P = nullptr, *d_pv = nullptr, *d_thr = nullptr;
+    int32_t *d_len = nullptr, *d_hof = nullptr;
+    unsigned long long *d_counts = nullptr;
+    int *d_status = nullptr;
+    const size_t pbytes = sizeof(float) * (size_t)p_rows * ncols;
+    cudaError_t e = cudaMallocAsync(&d_P, pbytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_len, sizeof(int32_t) * ncols, ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_hof, sizeof(int32_t) * ncols, ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_status, sizeof(int), ctx->stream);
+    if (e == cudaSuccess && npv > 0) e = cudaMallocAsync(&d_pv, sizeof(float) * npv, ctx->stream);
+    if (e == cudaSuccess && npv > 0) e = cudaMallocAsync(&d_thr, sizeof(float) * (size_t)npv * ncols, ctx->stream);
+    if (e == cudaSuccess && counts)
+        e = cudaMallocAsync(&d_counts, sizeof(unsigned long long) * (size_t)ncols * nbins, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_P, P, pbytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_len, col_len, sizeof(int32_t) * ncols, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_hof, hof.data(), sizeof(int32_t) * ncols, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && npv > 0)
+        e = cudaMemcpyAsync(d_pv, pvalues, sizeof(float) * npv, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(theoretical_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int status = 0;
+    if (e == cudaSuccess) {
+        TheoHistParams p{};
+        p.P = d_P;
+        p.p_rows = p_rows;
+        p.ncols = ncols;
+        p.col_len = d_len;
+        p.hist_of = d_hof;
+        for (int k = 0; k < 4; ++k) p.bg[k] = bg_prob[k];
+        p.nbins = nbins;
+        p.max_length = max_length;
+        p.fp64_dp = fp64_dp ? 1 : 0;
+        p.kmax = kmax;
+        p.pvalues = d_pv;
+        p.npv = npv;
+        p.thr = d_thr;
+        p.counts = d_counts;
+        p.status = d_status;
+        theoretical_hist_kernel<<<ncols, 256, smem, ctx->stream>>>(p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && npv > 0)
+        e = cudaMemcpyAsync(thr, d_thr, sizeof(float) * (size_t)npv * ncols, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && counts)
+        e = cudaMemcpyAsync(counts, d_counts, sizeof(unsigned long long) * (size_t)ncols * nbins,
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    void *bufs[] = {d_P, d_len, d_hof, d_status, d_pv, d_thr, d_counts};
+    for (void *b : bufs)
+        if (b) cudaFreeAsync(b, ctx->stream);
+    const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "theoretical histograms: %s", cudaGetErrorString(e));
+    if (status) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "a score range exceeds %d keys (fewer bins)", kmax);
+    return BLAMM_OK;
 }
 
 }  // extern "C"

@@ -153,6 +153,23 @@ int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4],
     });
 }
 
+int blamm_bank_hist_columns(const blamm_bank *bank, int32_t *hist_of)
+{
+    if (!bank || !hist_of) return -1;
+    return guarded([&] {
+        std::map<std::string, int32_t> fwd;  // base name -> first forward column
+        for (size_t c = 0; c < bank->motifs.size(); ++c) {
+            const blamm::Motif &m = bank->motifs[c];
+            if (!m.isRevCompl() && !fwd.count(m.baseName())) fwd[m.baseName()] = (int32_t)c;
+        }
+        for (size_t c = 0; c < bank->motifs.size(); ++c) {
+            auto it = fwd.find(bank->motifs[c].baseName());
+            if (it == fwd.end()) throw std::runtime_error("no forward motif for " + bank->motifs[c].baseName());
+            hist_of[c] = it->second;
+        }
+    });
+}
+
 const char *blamm_bank_name(const blamm_bank *bank, int c)
 {
     if (!bank || c < 0 || (size_t)c >= bank->motifs.size()) return nullptr;

@@ -18,6 +18,7 @@
 namespace blamm {
 
 constexpr int kStreamPad = 2048;   // padding bases after the stream end
+constexpr int kMaxMotifLen = 1024; // longest motif (the plain kernel reads up to 255 + L bases past a block)
 constexpr int kColBits = 20;       // tensor-core candidate = pos << 20 | tile slot
 
 // ------------------------------------------------------------------------
@@ -90,6 +91,7 @@ struct PlainParams {
     int32_t lmax;
     const int32_t *col_len;
     const float *thr;
+    const int32_t *cols;  // the ncols bank columns to scan (nullptr: columns 0 .. ncols-1)
     void *hits;  // blamm_hit*
     unsigned long long *hit_count;
     int64_t hit_cap;
@@ -135,11 +137,15 @@ __global__ void __launch_bounds__(256) scan_plain_kernel(PlainParams p)
     const int64_t p0 = (int64_t)blockIdx.x * blockDim.x;
     const int c0 = blockIdx.y * cpb;
     const int nc = min(cpb, p.ncols - c0);
-    for (int i = threadIdx.x; i < nc * p.p_rows; i += blockDim.x)
-        sP[i] = p.P[(size_t)c0 * p.p_rows + i];
+    for (int i = threadIdx.x; i < nc * p.p_rows; i += blockDim.x) {
+        const int cc = i / p.p_rows;
+        const int col = p.cols ? p.cols[c0 + cc] : c0 + cc;
+        sP[i] = p.P[(size_t)col * p.p_rows + (i - cc * p.p_rows)];
+    }
     for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-        sLen[i] = p.col_len[c0 + i];
-        sThr[i] = p.thr[c0 + i];
+        const int col = p.cols ? p.cols[c0 + i] : c0 + i;
+        sLen[i] = p.col_len[col];
+        sThr[i] = p.thr[col];
     }
     const int nwin = blockDim.x + p.lmax;
     for (int i = threadIdx.x; i < nwin; i += blockDim.x)
@@ -162,8 +168,8 @@ __global__ void __launch_bounds__(256) scan_plain_kernel(PlainParams p)
             }
             hit = s >= sThr[cc];
         }
-        emit_hits_warp(hit, pos, c0 + cc, s, reinterpret_cast<HitRec *>(p.hits), p.hit_count,
-                       p.hit_cap);
+        emit_hits_warp(hit, pos, p.cols ? p.cols[c0 + cc] : c0 + cc, s, reinterpret_cast<HitRec *>(p.hits),
+                       p.hit_count, p.hit_cap);
     }
 }
 

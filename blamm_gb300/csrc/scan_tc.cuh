@@ -29,8 +29,9 @@
 // group = warp / 4) and test sign bits; warp 16 allocates TMEM and one lane
 // issues the MMAs and the TMA bulk copies of B tiles; warps 17-19 build E from
 // 2-bit code windows that one of their threads prefetches with TMA bulk copies
-// kCodeStages jobs ahead.  kEStages E stages and two TMEM accumulators keep the roles
-// overlapped.
+// kCodeStages jobs ahead.  kEStages E stages and 2 or 4 TMEM accumulator stages (4 when
+// the plan's N tiles are at most 128 wide) keep the roles overlapped: the MMA warp may
+// run several jobs ahead of the drain.
 // Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
 // major, so a CTA reloads B only when its tile changes.  Every wait is
 // bounded: on a timeout the CTA raises an abort flag, every role stops,
@@ -53,7 +54,8 @@ constexpr int kEWarps = 3;       // E-builder warps 17-19
 constexpr int kEBarrier = 1;     // named barrier of the E builders
 constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps)
 constexpr int kCodeStages = 4;   // code windows in flight
-constexpr int kEStages = 4;      // one-hot E stages
+constexpr int kEStages = 6;      // one-hot E stages
+constexpr int kMaxAcc = 4;       // TMEM accumulator stages (at most)
 
 // Per-N-tile description (host-built, staged in SMEM by the kernel).
 struct TileDesc {
@@ -77,7 +79,8 @@ struct TcParams {
     const int32_t *slot_col;  // per slot: motif column, -1 for padding
     int32_t erows;       // E entries per stage (128 + 4 * max k-steps + 8)
     uint32_t b_term_max; // bytes reserved per B term in SMEM
-    uint32_t tmem_cols;  // TMEM columns allocated (2 accumulators)
+    uint32_t tmem_cols;  // TMEM columns allocated (acc_stages accumulators)
+    int32_t acc_stages;  // 2 (N <= 256) or 4 (N <= 128)
     unsigned long long *cand;
     unsigned long long *cand_count;
     int64_t cand_cap;
@@ -123,21 +126,23 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms,
     L.codes = take(kCodeStages * (code_seq_bytes(erows) + code_zm_bytes(erows)), 128);
     L.cand = take(kEpiWarps * kCandBuf * 8, 16);
     L.tiles = take((uint32_t)ntiles * sizeof(TileDesc), 16);
-    L.bars = take(32 * 8, 8);
+    L.bars = take(32 * 8, 8);  // BAR_COUNT <= 32
     L.misc = take(64, 16);
     L.total = take(0, 1024) + 1024;  // + slack for aligning the runtime base
     return L;
 }
 
 enum {
-    BAR_WFULL = 0,   // E stage built        (kEStages)
-    BAR_WEMPTY = 4,  // E stage consumed     (kEStages)
-    BAR_AFULL = 8,   // accumulator ready    (2)
-    BAR_AEMPTY = 10, // accumulator drained  (2)
-    BAR_BFULL = 12,  // B tile landed
-    BAR_DRAIN = 13,  // MMAs drained
-    BAR_CODE = 14    // code window landed   (kCodeStages)
+    BAR_WFULL = 0,                       // E stage built        (kEStages)
+    BAR_WEMPTY = BAR_WFULL + kEStages,   // E stage consumed     (kEStages)
+    BAR_AFULL = BAR_WEMPTY + kEStages,   // accumulator ready    (kMaxAcc)
+    BAR_AEMPTY = BAR_AFULL + kMaxAcc,    // accumulator drained  (kMaxAcc)
+    BAR_BFULL = BAR_AEMPTY + kMaxAcc,    // B tile landed
+    BAR_DRAIN = BAR_BFULL + 1,           // MMAs drained
+    BAR_CODE = BAR_DRAIN + 1,            // code window landed   (kCodeStages)
+    BAR_COUNT = BAR_CODE + kCodeStages
 };
+static_assert(BAR_COUNT <= 32, "the barrier area holds 32 mbarriers");
 
 // AND of 32 words as a shallow tree (3-input LOPs)
 __device__ __forceinline__ uint32_t and32(const uint32_t (&v)[32])
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             ptx::mbar_init(bars + 8 * (BAR_WFULL + s), 1);
             ptx::mbar_init(bars + 8 * (BAR_WEMPTY + s), 1);
         }
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < kMaxAcc; ++s) {
             ptx::mbar_init(bars + 8 * (BAR_AFULL + s), 1);
             ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps);
         }
@@ -289,7 +294,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem_base = *s_tmem;
-    const uint32_t acc_stride = p.tmem_cols >> 1;
+    const uint32_t acc_stride = p.tmem_cols / (uint32_t)p.acc_stages;
+    const uint32_t acc_shift = p.acc_stages == 4 ? 2u : 1u, acc_mask = (uint32_t)p.acc_stages - 1u;
     const long long njobs = (long long)p.ntiles * p.n_mtiles;
 
     if (warp == kMmaWarp) {
@@ -332,7 +338,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
                     bdesc_lo0 = ptx::smem_desc(sbase + L.b_lo, 128u, sbo_b);
                 }
-                const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;                   // accumulator
+                const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;     // accumulator
                 const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
                 const long long t0 = tick<kProf>();
                 ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
@@ -470,7 +476,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const int tile = it.tile;
             const int64_t m = it.m;
             const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
-            const uint32_t s = jc & 1u, ph = (jc >> 1) & 1u;
+            const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
             if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
             const long long t1 = tick<kProf>();

@@ -8,6 +8,9 @@ The reference ships no benchmark data; these generators stand in for it:
             1 % of bases in N runs of length log-uniform 100-10k
   config 4  10,000 sequences, log-normal lengths (median 2 kbp, sigma 1.0,
             clipped 200-50k), GC 0.5, 800 motifs (L 6-25)
+  config 5  serving: a resident bank of 2000 motifs (L 5-30); requests of log-uniform
+            length 1 kbp-5 Mbp (iid, GC ~ U[0.35, 0.6]), a subset of U{1..2000}
+            motifs and p in {1e-3, 1e-4, 1e-5}
 Motif columns are Multinomial(100, Dirichlet(0.5 * 1_4)) counts.  Random
 streams: numpy default_rng with separate children for motifs, lengths, bases.
 """
@@ -132,6 +135,28 @@ def config4(seed: int = 0, nseq: int = 10_000) -> Workload:
     lens = np.clip(np.round(np.exp(rl.normal(np.log(2000), 1.0, size=nseq))), 200, 50_000).astype(np.int64)
     seqs = [(f"prom{i}", iid_bases(rb, int(L), [0.25, 0.25, 0.25, 0.25])) for i, L in enumerate(lens)]
     return Workload("config4", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+
+
+def config5_bank(seed: int = 0) -> list[tuple[str, np.ndarray]]:
+    rm, _, _ = rngs(seed)
+    return random_pfms(rm, 2000, 5, 30)
+
+
+CONFIG5_PVALUES = (1e-3, 1e-4, 1e-5)
+
+
+def config5_requests(seed: int, k: int, nmotifs: int = 2000, max_len: int = 5_000_000):
+    """k serving requests: (bases, run starts [0], motif indices (sorted), p-value index)."""
+    rng = np.random.default_rng([seed, 5])
+    out = []
+    for _ in range(k):
+        n = int(np.exp(rng.uniform(np.log(1_000), np.log(max_len))))
+        gc = rng.uniform(0.35, 0.6)
+        b = iid_bases(rng, n, [(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])
+        m = int(rng.integers(1, nmotifs + 1))
+        motifs = np.sort(rng.choice(nmotifs, size=m, replace=False))
+        out.append((b, np.zeros(1, dtype=np.int64), motifs, int(rng.integers(0, len(CONFIG5_PVALUES)))))
+    return out
 
 
 # ---------------------------------------------------------------- writers

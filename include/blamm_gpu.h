@@ -92,6 +92,12 @@ int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols,
 /* Replace the thresholds only (per species / per p-value), keeping the bank. */
 int blamm_set_thresholds(blamm_ctx *ctx, const float *thr);
 
+/* Scan only the n bank columns cols[0..n-1] (distinct, each in [0, ncols));
+ * n = 0 scans every column again.  Hits keep the bank's column numbers.  The
+ * reference always scans its whole bank; a subset serves requests that ask
+ * for some motifs only.  blamm_set_motifs resets the subset. */
+int blamm_set_columns(blamm_ctx *ctx, const int32_t *cols, int n);
+
 /* Scan a filtered base stream held in host memory.
  * bases: n characters from {A,C,G,T,a,c,g,t} -- the content of the reference's
  *   SeqBlock stream (src/sequence.cpp:181-250).  Lowercase bases are scanned
@@ -118,8 +124,70 @@ int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n,
 int blamm_filter_score(blamm_ctx *ctx, float *d_R, int m, int n, const float *d_threshold,
                        int *d_occIdx, float *d_occScore, int *d_nOcc);
 
+/* Batched and graph launches (no counterpart in the reference, which
+ * synchronises after every sgemm batch, src/pwmscan.cpp:386-412).
+ *
+ * blamm_reserve sizes the context's buffers for scans of up to max_positions
+ * positions and max_candidates tensor-core candidates and builds the tile plan
+ * of the current bank, columns, thresholds and mode.  After it,
+ * blamm_scan_enqueue needs no allocation and no host synchronisation: it
+ * enqueues packing, the scan and the rescoring on the context's stream and
+ * returns.  counts is device memory of 4 uint64, set when the stream gets
+ * there: [0] candidates, [1] hits, [2] status (non-zero: a device wait timed
+ * out).  Hits beyond hit_cap and candidates beyond the reservation are counted
+ * but not stored; the caller compares counts with its capacities and scans
+ * again with more room.  BLAMM_ERR_STATE when the reservation or plan does not
+ * cover the call.
+ *
+ * blamm_scan_graph_create captures one blamm_scan_enqueue into an executable
+ * CUDA graph (opaque handle) that blamm_scan_graph_launch replays on the
+ * context's stream.  The graph holds the buffer addresses of its capture: it
+ * stays valid until the bank, columns, thresholds, mode or reservation change
+ * or the context is destroyed. */
+int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates);
+int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
+                       int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, uint64_t *d_counts);
+int blamm_scan_graph_create(blamm_ctx *ctx, const char *d_bases, int64_t n,
+                            const int64_t *d_run_start, int64_t nruns, blamm_hit *d_hits,
+                            int64_t hit_cap, uint64_t *d_counts, void **graph);
+int blamm_scan_graph_launch(blamm_ctx *ctx, void *graph);
+void blamm_scan_graph_destroy(void *graph);
+
+/* Autotuner: time the tensor-core scan of the first min(n, 16 Mi) positions
+ * (device data) under several tile plans -- widest N tile 128 / 192 / 256 x
+ * the planner's fixed cost per job -- and keep the fastest plan for later
+ * scans of this context.  *best_ms (optional) receives its kernel time.
+ * Nothing to tune in BLAMM_MODE_FP32. */
+int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
+                   int64_t nruns, float *best_ms);
+
+/* The planner's knobs that the autotuner sets: the widest N tile (32..256
+ * columns; at most 128 gives four TMEM accumulators instead of two) and the
+ * fixed cycles per job of its cost model.  Setting them replans. */
+int blamm_set_plan_options(blamm_ctx *ctx, int max_tile_columns, float job_cost);
+int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *job_cost);
+
+/* The hist module's theoretical histograms and p-value thresholds on the GPU
+ * (Motif::computeTheoreticalSpectrum src/motif.cpp:151-192,
+ * Histogram::generateTheoreticalHist src/hist.cpp:162-175,
+ * ScoreHistogram::getScoreCutoff src/motif.cpp:47-69), one CTA per column.
+ * Column c's distribution is that of column hist_of[c]'s PWM (NULL: its own;
+ * the reference gives a reverse-complement or permuted motif the histogram of
+ * its forward motif); bg_prob are the background probabilities, nbins <= 4096
+ * bins of max_length observations.  fp64_dp = 0 follows the reference's FP32
+ * dynamic programme operation for operation (same counts, same thresholds bit
+ * for bit); 1 runs it in FP64.  The inversion is FP64 as in the reference.
+ * Outputs (host memory, either may be NULL): thr, npv x ncols thresholds (row v
+ * for pvalues[v]); counts, ncols x nbins histogram counts. */
+int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols, const int32_t *col_len,
+                           const int32_t *hist_of, const float bg_prob[4], int nbins, uint64_t max_length,
+                           int fp64_dp, const float *pvalues, int npv, float *thr, uint64_t *counts);
+
 /* Number of CUDA devices (0 when there is no driver or device). */
 int blamm_device_count(int *n);
+
+/* Free and total device memory of a device (cudaMemGetInfo). */
+int blamm_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes);
 
 /* Soft-masked (lowercase) bases: 0 (default) = they add nothing to a score,
  * as in the reference's BLAS/cuBLAS scan (src/sequence.cpp:312-318);

@@ -54,6 +54,11 @@ int blamm_bank_min_max(const blamm_bank *bank, float *min_score, float *max_scor
 int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4], int nbins,
                                  uint64_t max_length, float pvalue, float *thr);
 
+/* For every column, the column of the forward motif whose histogram gives
+ * its p-value threshold (the same base name, src/motif.h:256-267): the
+ * hist_of argument of blamm_theoretical_hist. */
+int blamm_bank_hist_columns(const blamm_bank *bank, int32_t *hist_of);
+
 /* Name of column c (valid until the bank is freed). */
 const char *blamm_bank_name(const blamm_bank *bank, int c);
 

@@ -117,7 +117,7 @@ def test_fasta_chunks_equal_oracle_stream(payload, overlap, max_filt):
 
 def test_every_declared_symbol_is_exported():
     from blamm_gb300._native import gpu_lib, host_lib
-    for header, lib in (("blamm_gpu.h", gpu_lib()), ("blamm_host.h", host_lib())):
+    for header, lib in (("blamm_gpu.h", gpu_lib()), ("blamm_host.h", host_lib()), ("blamm_serve.h", host_lib())):
         text = open(os.path.join(ROOT, "include", header)).read()
         names = set(re.findall(r"^[A-Za-z_][\w \*]*?\b(blamm_\w+)\s*\(", text, flags=re.M))
         assert len(names) > 5
