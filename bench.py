@@ -207,6 +207,30 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ precision of the MMA scores
+def mma_score_error(sc, bases, P, lens, npos: int = 2048) -> dict:
+    """Raw tensor-core scores (sum of the fixed-point BF16 terms, before rescoring) of the first
+    npos positions x every column, against the FP64 sum of the FP32 PWM entries."""
+    bases = bases[:npos + 256]
+    raw = sc.debug_scores(bases, 0, npos).astype(np.float64)
+    code = np.full(len(bases) + 512, 4, dtype=np.int64)
+    for v, ch in enumerate(b"ACGT"):
+        code[:len(bases)][bases == ch] = v
+    ncols = P.shape[0]
+    ref = np.zeros((npos, ncols), dtype=np.float64)
+    Pz = np.concatenate([P.astype(np.float64), np.zeros((ncols, 4))], axis=1)
+    zero = P.shape[1]
+    for c in range(ncols):
+        for j in range(int(lens[c])):
+            b = code[j:j + npos]
+            ref[:, c] += Pz[c, np.where(b < 4, 4 * j + b, zero)]
+    valid = (np.arange(npos)[:, None] + lens[None, :]) <= len(bases)
+    err = np.abs(raw - ref)[valid]
+    rel = (np.abs(raw - ref) / np.maximum(np.abs(ref), 1.0))[valid]
+    return {"positions": npos, "columns": int(ncols), "max_abs": float(err.max()), "mean_abs": float(err.mean()),
+            "max_rel": float(rel.max()), "rel_denominator": "max(|fp64 score|, 1)"}
+
+
 # ------------------------------------------------------------------ serving (config 5)
 def run_serve(a) -> dict:
     """Config-5 serving through the scan service (include/blamm_serve.h): a resident bank of
@@ -386,6 +410,14 @@ def run_ours(a, rank, world, local):
                            "same_hits_as_bf16x2": hit_digest(hits_on_device(mnh)) == ref_digest}
         sc.set_mode("bf16x2")
 
+    # ---- score error of the tensor-core sums against FP64 (emitted scores are rescored in FP32)
+    precision = {}
+    if rank == 0:
+        for mode in ("bf16x2", "bf16"):
+            sc.set_mode(mode)
+            precision[mode] = mma_score_error(sc, bases, P, lens)
+        sc.set_mode("bf16x2")
+
     # ---- roofline of the dominant kernel (tcgen05 scan)
     peak, peak_src = peaks()
     kern_ms = float(np.mean(scan_ms))
@@ -414,6 +446,7 @@ def run_ours(a, rank, world, local):
                      "note": f"algorithmic flops = 8 * sum(L) = {flops_per_bp:.0f} per bp per launch over "
                              f"{n} bp; the hi+lo split issues 2 MMAs per flop (ceiling 0.5); peak {peak_src}"},
         "modes": modes,
+        "mma_score_error_vs_fp64": precision,
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not a.no_serve:

@@ -65,7 +65,7 @@ struct blamm_ctx {
     size_t cap_tiles = 0, cap_bbuf = 0, cap_slot_col = 0;
     // planner knobs (the autotuner sets them): widest N tile, fixed cycles per job
     int plan_nmax = 256;
-    double plan_job_cost = 200.0;
+    double plan_job_cost = 700.0;
 
     // stream buffers
     char *d_bases = nullptr;
