@@ -49,6 +49,9 @@ def args_parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-requests", type=int, default=48, help="distinct requests of the serving pool")
     ap.add_argument("--serve-slots", type=int, default=8, help="requests in flight in the serving measurement")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4"],
+                    help="config2 is the headline line; config3 (1 Gbp x 2000 motifs, precision at scale) and "
+                         "config4 (10,000 short sequences, batching) print their own measurement line")
     return ap.parse_args()
 
 
@@ -299,6 +302,170 @@ def run_serve(a) -> dict:
         srv.close()
 
 
+# ------------------------------------------------------------------ configs 3 and 4
+def _bank_for(pfms, counts, pvalues, sc):
+    """Bank (rc interleaved) + thresholds per p-value from GPU theoretical histograms."""
+    from blamm_gb300._native import MotifBank
+    bank = MotifBank.from_pfms([p for _, p in pfms], revcompl=True)
+    bank.generate(counts, 0.25)
+    P, lens, _ = bank.matrix()
+    bgp = ((counts.astype(np.float32) + np.float32(0.25)) /
+           (np.float32(counts.sum()) + np.float32(1.0))).astype(np.float32)
+    t0 = time.perf_counter()
+    thr, _ = sc.theoretical_hist(P, lens, bgp, pvalues, hist_of=bank.hist_columns())
+    t_gpu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    host = bank.pvalue_thresholds(bgp, pvalues[0])
+    t_host = time.perf_counter() - t0
+    same = bool(np.array_equal(host.view(np.uint32), thr[0].view(np.uint32)))
+    return P, lens, thr, {"gpu_s_all_pvalues": t_gpu, "host_s_one_pvalue": t_host, "gpu_equals_host": same}
+
+
+def _device_scan(sc, torch, d_b, n, d_r, nr, cap):
+    from blamm_gb300 import HIT_DTYPE
+    d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), nr, d_h.data_ptr(), cap)
+    return nh, d_h
+
+
+def run_config3(a):
+    """Config 3: 2000 motifs (4000 columns) over 1 Gbp (2nd-order Markov, GC 0.41, 1 % N runs),
+    p = 1e-4 and 1e-5 thresholds inverted in FP64 on the GPU; BF16 split vs single-term BF16
+    (same hits required); the plain FP32 form on a 100 Mbp sample."""
+    import torch
+    from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
+    t0 = time.perf_counter()
+    wl = workloads.config3(a.seed, total=a.bases if a.bases != 100_000_000 else 1_000_000_000)
+    bases, runs, _, _ = workloads.filtered_stream(wl.sequences)
+    gen_s = time.perf_counter() - t0
+    counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
+    sc = GpuScanner(0, "bf16x2")
+    P, lens, thr, tinfo = _bank_for(wl.motifs, counts, (1e-4, 1e-5), sc)
+    n, ncols = len(bases), P.shape[0]
+    d_b = torch.from_numpy(bases).cuda()
+    d_r = torch.from_numpy(runs).cuda()
+    out = {"workload": f"config3: 2000 motifs (4000 columns) x {n} bp (2nd-order Markov, GC 0.41, 1% N runs), "
+                       "thresholds from GPU theoretical histograms (FP64 inversion)",
+           "generate_s": gen_s, "thresholds": tinfo, "runs": []}
+    for pi, pv in enumerate((1e-4, 1e-5)):
+        sc.set_motifs(P, lens, thr[pi])
+        res = {"pvalue": pv}
+        digests = {}
+        for mode in ("bf16x2", "bf16"):
+            sc.set_mode(mode)
+            from blamm_gb300 import HIT_DTYPE as HD
+            nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), 0, 0, overflow_ok=True)
+            cap = nh + 1024
+            d_h = torch.empty(cap * HD.itemsize, dtype=torch.uint8, device="cuda")
+            ts = []
+            for _ in range(3):
+                nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+                ts.append(sc.stats())
+            st = ts[-1]
+            h = d_h[: nh * HD.itemsize].cpu().numpy().view(HD)
+            digests[mode] = hit_digest(h)
+            kern = float(np.median([t["scan_ms"] for t in ts]))
+            tot = float(np.median([t["kernel_ms"] for t in ts]))
+            res[mode] = {"hits": int(nh), "candidates": int(st["candidates"]), "scan_kernel_ms": kern,
+                         "all_kernels_ms": tot, "bp_motif_per_s": n * ncols / (tot / 1e3),
+                         "tiles": int(st["tiles"])}
+            del d_h
+        res["same_hits_bf16_vs_bf16x2"] = digests["bf16"] == digests["bf16x2"]
+        out["runs"].append(res)
+    # plain FP32 form on a 100 Mbp sample of the same stream, same hits as the split there
+    m = min(n, 100_000_000)
+    rs = runs[runs < m]
+    sc.set_motifs(P, lens, thr[0])
+    sample = {}
+    for mode in ("fp32", "bf16x2"):
+        sc.set_mode(mode)
+        from blamm_gb300 import HIT_DTYPE as HD
+        d_rs = torch.from_numpy(rs).cuda()
+        cap = sc.scan_device(d_b.data_ptr(), m, d_rs.data_ptr(), len(rs), 0, 0, overflow_ok=True) + 1024
+        d_h = torch.empty(cap * HD.itemsize, dtype=torch.uint8, device="cuda")
+        nh = sc.scan_device(d_b.data_ptr(), m, d_rs.data_ptr(), len(rs), d_h.data_ptr(), cap)
+        st = sc.stats()
+        sample[mode] = {"hits": int(nh), "kernel_ms": float(st["kernel_ms"]),
+                        "bp_motif_per_s": m * ncols / (st["kernel_ms"] / 1e3),
+                        "digest": hit_digest(d_h[: nh * HD.itemsize].cpu().numpy().view(HD))}
+        del d_h
+    sample["same_hits"] = sample["fp32"].pop("digest") == sample["bf16x2"].pop("digest")
+    sample["bases"] = m
+    out["fp32_sample_p1e-4"] = sample
+    sc.close()
+    print(json.dumps({"metric": METRIC, "config": out}), flush=True)
+
+
+def run_config4(a):
+    """Config 4: 10,000 promoter-like sequences (log-normal lengths, median 2 kbp, sigma 1.0,
+    clipped 200 bp-50 kbp, GC 0.5) x 800 motifs (1600 columns), p = 1e-4: one persistent launch
+    over all sequences, the same as a CUDA graph, and one launch per sequence; autotuned plan."""
+    import torch
+    from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
+    wl = workloads.config4(a.seed)
+    bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
+    counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
+    sc = GpuScanner(0, "bf16x2")
+    P, lens, thr, _ = _bank_for(wl.motifs, counts, (1e-4,), sc)
+    sc.set_motifs(P, lens, thr[0])
+    n, ncols = len(bases), P.shape[0]
+    units = n * ncols
+    d_b = torch.from_numpy(bases).cuda()
+    d_r = torch.from_numpy(runs).cuda()
+    cap = max(1 << 20, units // 1000)
+    d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    ext = torch.cuda.ExternalStream(sc.stream())
+
+    def timed(fn, reps=5):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            fn()
+            e1.record(ext)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    one = timed(lambda: sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap))
+    nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+    batch = hit_digest(d_h[: nh * HIT_DTYPE.itemsize].cpu().numpy().view(HIT_DTYPE))
+    # a CUDA graph of the enqueued scan
+    sc.reserve(n, cap)
+    d_c = torch.zeros(4, dtype=torch.int64, device="cuda")
+    g = sc.graph_create(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap, d_c.data_ptr())
+    graph_ms = timed(lambda: sc.graph_launch(g))
+    sc.graph_destroy(g)
+    # one launch per sequence (host loop, synchronous calls), on a share of the sequences
+    seq_start = np.concatenate([[0], np.cumsum([len(s) for _, s in wl.sequences])])
+    k = min(len(wl.sequences), 2000)
+    d_one = torch.zeros(1, dtype=torch.int64, device="cuda")
+    t0 = time.perf_counter()
+    per_hits = 0
+    for i in range(k):
+        a0, a1 = int(seq_start[i]), int(seq_start[i + 1])
+        per_hits += sc.scan_device(d_b.data_ptr() + a0, a1 - a0, d_one.data_ptr(), 1, d_h.data_ptr(), cap)
+    torch.cuda.synchronize()
+    per_seq_ms = (time.perf_counter() - t0) * 1e3 * len(wl.sequences) / k
+    # the autotuned plan
+    best = sc.autotune(d_b.data_ptr(), n, d_r.data_ptr(), len(runs))
+    tuned = timed(lambda: sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap))
+    nh2 = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+    same = hit_digest(d_h[: nh2 * HIT_DTYPE.itemsize].cpu().numpy().view(HIT_DTYPE)) == batch
+    out = {"workload": f"config4: {len(wl.sequences)} sequences ({n} bp) x 800 motifs (1600 columns), p=1e-4",
+           "one_launch_ms": one, "one_launch_bp_motif_per_s": units / (one / 1e3),
+           "graph_ms": graph_ms, "graph_bp_motif_per_s": units / (graph_ms / 1e3),
+           "per_sequence_launches_ms": per_seq_ms, "per_sequence_bp_motif_per_s": units / (per_seq_ms / 1e3),
+           "per_sequence_sample": f"first {k} sequences, extrapolated to all",
+           "autotuned_ms": tuned, "autotune_plan": list(sc.plan_options()), "autotuned_same_hits": same,
+           "hits": int(nh)}
+    sc.close()
+    print(json.dumps({"metric": METRIC, "config": out}), flush=True)
+
+
 # ------------------------------------------------------------------ GPU side
 def run_ours(a, rank, world, local):
     import torch
@@ -473,6 +640,14 @@ def main():
     rank, world, local = dist_env()
     if a.impl == "reference":
         run_reference(a, rank, world)
+        return
+    if a.workload == "config3":
+        if rank == 0:
+            run_config3(a)
+        return
+    if a.workload == "config4":
+        if rank == 0:
+            run_config4(a)
         return
     run_ours(a, rank, world, local)
 

@@ -172,12 +172,15 @@ class GpuScanner:
             return out[: nh.value]
 
     def scan_device(self, d_bases: int, n: int, d_runs: int, nruns: int, d_hits: int,
-                    hit_cap: int) -> int:
-        """Device pointers in, device hits out; returns the hit count."""
+                    hit_cap: int, overflow_ok: bool = False) -> int:
+        """Device pointers in, device hits out; returns the hit count (with overflow_ok, a
+        count above hit_cap instead of an error: only hit_cap hits were stored)."""
         nh = C.c_int64(0)
         rc = self.lib.blamm_scan_device(self.h, C.c_void_p(d_bases), n, C.c_void_p(d_runs), nruns,
                                         C.c_void_p(d_hits), hit_cap, C.byref(nh))
         if rc == BLAMM_ERR_OVERFLOW:
+            if overflow_ok:
+                return nh.value
             raise BlammError(rc, f"{nh.value} hits exceed the capacity {hit_cap}")
         self._check(rc)
         return nh.value

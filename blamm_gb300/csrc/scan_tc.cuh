@@ -194,20 +194,30 @@ __device__ __noinline__ int flush_candidates(int lane, unsigned long long *buf, 
 
 // Stage the candidates of one 32-column chunk (mask bit i = column slot0 + i of this
 // lane's position) in the warp's SMEM buffer; returns the new fill.  Warp-collective.
+// The usual case -- no lane with more than one candidate -- takes its offsets from one
+// ballot; otherwise an inclusive scan over the lanes' counts.
 __device__ __forceinline__ int stage_candidates(uint32_t mask, int slot0, int64_t pos, int lane, unsigned long long *buf,
                                              int fill, unsigned long long *cand, unsigned long long *cand_count,
                                              int64_t cand_cap)
 {
     const int cnt = __popc(mask);
-    int incl = cnt;
+    int at, total;
+    const uint32_t lt = (1u << lane) - 1u;
+    if (__ballot_sync(0xffffffffu, cnt > 1) == 0u) {
+        const uint32_t one = __ballot_sync(0xffffffffu, cnt == 1);
+        at = __popc(one & lt);
+        total = __popc(one);
+    } else {
+        int incl = cnt;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        total = __shfl_sync(0xffffffffu, incl, 31);
+        at = incl - cnt;
     }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
     if (total == 0) return fill;
-    int at = incl - cnt;
     if (fill + total > kCandBuf) fill = flush_candidates(lane, buf, fill, cand, cand_count, cand_cap);
     const unsigned long long key = (unsigned long long)pos << kColBits;
     if (total > kCandBuf) {  // more than a buffer: straight to global memory
@@ -233,7 +243,6 @@ __device__ __forceinline__ int stage_candidates(uint32_t mask, int slot0, int64_
     return fill + total;
 }
 
-// Clock read for the role timing; compiled out (0) when kProf is false.
 template <bool kProf>
 __device__ __forceinline__ long long tick()
 {

@@ -46,28 +46,36 @@ def iid_bases(rng: np.random.Generator, n: int, probs) -> np.ndarray:
     return ACGT[idx]
 
 
-def markov2_bases(rng: np.random.Generator, n: int, gc: float = 0.41) -> np.ndarray:
-    """2nd-order Markov chain: seeded 16 x 4 transition table, rows tilted to the GC target."""
-    table = rng.dirichlet([2.0] * 4, size=16)
+def markov2_bases(rng: np.random.Generator, n: int, gc: float = 0.41, block: int = 1000) -> np.ndarray:
+    """2nd-order Markov chain: seeded 16 x 4 transition table, rows tilted to the GC target.
+
+    Sampled as n / block independent chains of `block` bases advanced together (vectorised
+    over the chains); each chain starts from a uniformly drawn two-base context."""
+    raw = rng.dirichlet([2.0] * 4, size=16)
     target = np.array([(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])
-    table = table * target
-    table /= table.sum(axis=1, keepdims=True)
-    cdf = np.cumsum(table, axis=1)
-    u = rng.random(n)
-    out = np.empty(n, dtype=np.uint8)
-    # vectorised in chunks: the state depends on the previous two symbols only
-    state = 0
-    chunk = 1 << 16
-    codes = np.empty(n, dtype=np.uint8)
-    for s in range(0, n, chunk):
-        e = min(n, s + chunk)
-        for i in range(s, e):
-            c = int(np.searchsorted(cdf[state], u[i], side="right"))
-            c = min(c, 3)
-            codes[i] = c
-            state = ((state << 2) | c) & 15
-    out[:] = ACGT[codes]
-    return out
+    w = target.copy()
+    for _ in range(20):  # tilt the rows until the chain's stationary base composition hits the target
+        table = raw * w
+        table /= table.sum(axis=1, keepdims=True)
+        T = np.zeros((16, 16))
+        for st in range(16):
+            for c in range(4):
+                T[st, ((st << 2) | c) & 15] += table[st, c]
+        pi = np.full(16, 1 / 16)
+        for _ in range(200):
+            pi = pi @ T
+        comp = np.array([pi[np.arange(16) & 3 == c].sum() for c in range(4)])
+        w *= target / comp
+    cdf = np.cumsum(table, axis=1)[:, :3]  # symbol = number of cdf entries below u
+    nb = (n + block - 1) // block
+    state = rng.integers(0, 16, size=nb)
+    codes = np.empty((nb, block), dtype=np.uint8)
+    for i in range(block):
+        u = rng.random(nb)
+        c = (u[:, None] >= cdf[state]).sum(axis=1)
+        codes[:, i] = c
+        state = ((state << 2) | c) & 15
+    return ACGT[codes.reshape(-1)[:n]]
 
 
 def insert_n_runs(rng: np.random.Generator, seq: np.ndarray, frac: float, lmin: int = 100,
@@ -122,9 +130,7 @@ def config3(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Worklo
     lens = np.maximum(1, np.round(raw / raw.sum() * total)).astype(np.int64)
     seqs = []
     for i, L in enumerate(lens):
-        # iid with GC 0.41 stands in for the Markov chain at full size (python loop too slow);
-        # markov2_bases() is used at reduced sizes
-        s = iid_bases(rb, int(L), [0.295, 0.205, 0.205, 0.295])
+        s = markov2_bases(rb, int(L), 0.41)
         seqs.append((f"chr{i + 1}", insert_n_runs(rb, s, 0.01)))
     return Workload("config3", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
 

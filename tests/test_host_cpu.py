@@ -144,3 +144,19 @@ def test_cli_errors_match_reference_behaviour(tmp_path):
         f.write("sp\tbad.fa\n")
     r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=d, capture_output=True)
     assert r.returncode == 1 and b"does not appear to be in fasta format" in r.stderr
+
+
+def test_bank_hist_columns_map_rc_columns_to_their_forward_motif():
+    """blamm_bank_hist_columns: each column's histogram comes from its forward motif
+    (the same base name), as the reference's hist files are named (src/motif.h:256-267)."""
+    rng = np.random.default_rng(12)
+    pf = [p for _, p in workloads.random_pfms(rng, 20, 5, 15)]
+    bank = MotifBank.from_pfms(pf, revcompl=True)
+    bank.generate(np.array([30, 20, 20, 30], dtype=np.uint64), 0.25)
+    _, _, rc = bank.matrix()
+    hof = bank.hist_columns()
+    for c in range(bank.columns):
+        h = int(hof[c])
+        assert rc[h] == 0 and bank.name(h) == bank.name(c).replace("_rc", "")[: len(bank.name(h))]
+        if rc[c] == 0:
+            assert h == c
