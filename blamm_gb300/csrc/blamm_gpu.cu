@@ -20,6 +20,7 @@
 #include "scan_kernels.cuh"
 #include "scan_tc.cuh"
 #include "hist_kernels.cuh"
+#include "ingest_kernels.cuh"
 
 using namespace blamm;
 
@@ -1522,6 +1523,118 @@ int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "theoretical histograms: %s", cudaGetErrorString(e));
     if (status) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "a score range exceeds %d keys (fewer bins)", kmax);
+    return BLAMM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ FASTA ingest on the GPU
+
+// In-place inclusive scan of v[0..n) with Op; `scratch` holds at least
+// scan_scratch_words(n) values.
+static size_t scan_scratch_words(int64_t n)
+{
+    size_t w = 0;
+    for (int64_t t = (n + kScanTile - 1) / kScanTile; t > 1; t = (t + kScanTile - 1) / kScanTile) w += (size_t)t;
+    return w + 1;
+}
+
+template <class Op>
+static cudaError_t device_scan(cudaStream_t st, int64_t *v, int64_t n, int64_t *scratch)
+{
+    if (n <= 0) return cudaSuccess;
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    scan_tiles_kernel<Op><<<(unsigned)tiles, kScanThreads, 0, st>>>(v, n, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || tiles == 1) return e;
+    e = device_scan<Op>(st, scratch, tiles, scratch + tiles);
+    if (e != cudaSuccess) return e;
+    scan_add_kernel<Op><<<(unsigned)tiles, kScanThreads, 0, st>>>(v, n, scratch);
+    return cudaGetLastError();
+}
+
+extern "C" {
+
+int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
+                             int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
+                             int64_t *d_header_pos, int64_t *nseqs)
+{
+    if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs) return BLAMM_ERR_ARG;
+    *n_bases = *nruns = *nseqs = 0;
+    if (nraw == 0) return BLAMM_OK;
+    if (!d_raw || !d_bases || !d_run_start || !d_run_seq || !d_run_seqpos || !d_header_pos)
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)nraw, sw = scan_scratch_words(nraw);
+    // four per-byte arrays (line starts, header count, sequence characters, stream bases),
+    // the per-sequence character offsets, scan scratch and a status word
+    int64_t *A = nullptr, *B = nullptr, *Cc = nullptr, *D = nullptr, *sc0 = nullptr, *scr = nullptr;
+    int *bad = nullptr;
+    cudaError_t e = cudaMallocAsync(&A, 8 * n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&B, 8 * n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&Cc, 8 * n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&D, 8 * n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&sc0, 8 * n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&scr, 8 * sw, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&bad, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+    const unsigned grid = (unsigned)std::min<int64_t>((nraw + 255) / 256, (int64_t)ctx->sm_count * 32);
+    if (e == cudaSuccess) {
+        ingest_lines_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = device_scan<MaxOp>(st, A, nraw, scr);
+    if (e == cudaSuccess) e = device_scan<SumOp>(st, B, nraw, scr);
+    if (e == cudaSuccess) {
+        ingest_chars_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B, Cc, D, bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = device_scan<SumOp>(st, Cc, nraw, scr);
+    if (e == cudaSuccess) e = device_scan<SumOp>(st, D, nraw, scr);
+    int64_t tot[2] = {0, 0};
+    int badh = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[0], B + nraw - 1, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[1], D + nraw - 1, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&badh, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    const int64_t ns = tot[0], nb = tot[1];
+    if (e == cudaSuccess && !badh) {
+        ingest_headers_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, B, Cc, sc0, d_header_pos);
+        e = cudaGetLastError();
+    }
+    int64_t *bseq = nullptr, *bpos = nullptr;
+    if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bseq, 8 * (size_t)nb, st);
+    if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bpos, 8 * (size_t)nb, st);
+    if (e == cudaSuccess && !badh && nb > 0) {
+        ingest_bases_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B, Cc, D, sc0, d_bases, bseq, bpos);
+        e = cudaGetLastError();
+    }
+    int64_t nr = 0;
+    if (e == cudaSuccess && !badh && nb > 0) {
+        // run flags into A (no longer needed), scanned in place
+        const unsigned g2 = (unsigned)std::min<int64_t>((nb + 255) / 256, (int64_t)ctx->sm_count * 32);
+        ingest_runflags_kernel<<<g2, 256, 0, st>>>(bseq, bpos, nb, A);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = device_scan<SumOp>(st, A, nb, scr);
+        if (e == cudaSuccess) {
+            ingest_runs_kernel<<<g2, 256, 0, st>>>(bseq, bpos, nb, A, d_run_start, d_run_seq, d_run_seqpos);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&nr, A + nb - 1, 8, cudaMemcpyDeviceToHost, st);
+    }
+    void *bufs[] = {A, B, Cc, D, sc0, scr, bad, bseq, bpos};
+    for (void *b : bufs)
+        if (b) cudaFreeAsync(b, st);
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess)
+        return fail(ctx, e == cudaErrorMemoryAllocation ? BLAMM_ERR_NOMEM : BLAMM_ERR_CUDA, "FASTA ingest: %s",
+                    cudaGetErrorString(e));
+    if (badh) return fail(ctx, BLAMM_ERR_ARG, "Input file does not appear to be in fasta format");
+    *n_bases = nb;
+    *nruns = nr;
+    *nseqs = ns;
     return BLAMM_OK;
 }
 

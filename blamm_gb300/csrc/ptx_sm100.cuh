@@ -34,22 +34,26 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t byt
                  : "memory");
 }
 
+// A waiting thread sleeps until the phase completes or this many nanoseconds
+// pass (a hint), instead of spinning: idle roles leave the issue slots to the
+// working warps of their SM sub-partition.
+constexpr uint32_t kTryWaitSleepNs = 20000;
+
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "n"(kTryWaitSleepNs)
         : "memory");
     return ok != 0;
 }
 
-// Bounded wait: spins on try_wait (which itself suspends for a
-// hardware-chosen interval), polls the CTA abort flag, and gives up after
-// `limit_cycles`.  Returns false on timeout or abort; on timeout it raises the
+// Bounded wait: repeats try_wait (each sleeps at most kTryWaitSleepNs), polls
+// the CTA abort flag every 8 tries, and gives up after `limit_cycles`.  Returns false on timeout or abort; on timeout it raises the
 // abort flag so that every other role of the CTA stops waiting too.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
                                           long long limit_cycles)
@@ -58,7 +62,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
     const long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63u) == 0) {
+        if ((it & 7u) == 0) {
             if (*abort_flag) return false;
             if (clock64() - t0 > limit_cycles) {
                 *abort_flag = 1;

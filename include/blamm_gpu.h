@@ -183,6 +183,19 @@ int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols
                            const int32_t *hist_of, const float bg_prob[4], int nbins, uint64_t max_length,
                            int fp64_dp, const float *pvalues, int npv, float *thr, uint64_t *counts);
 
+/* FASTA ingest on the GPU: the filtered base stream and run table that
+ * FastaBatch builds (src/sequence.cpp:142-293) from raw FASTA text in device
+ * memory (several files concatenated, each ending with a newline).  Outputs,
+ * device memory sized for the worst case (nraw entries each): the stream
+ * bases (A/C/G/T/a/c/g/t), per run its stream start, sequence index and
+ * position in the sequence (the SeqBlock markers, src/sequence.cpp:35-50),
+ * and per sequence the byte offset of its '>' header line (names stay with
+ * the caller).  Counts come back in *n_bases, *nruns, *nseqs.  Sequence data
+ * before the first header gives BLAMM_ERR_ARG, as the reference rejects it. */
+int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
+                             int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
+                             int64_t *d_header_pos, int64_t *nseqs);
+
 /* Number of CUDA devices (0 when there is no driver or device). */
 int blamm_device_count(int *n);
 

@@ -1,0 +1,79 @@
+"""GPU FASTA ingest (blamm_fasta_parse_device) against the oracle's restatement of
+FastaBatch: same stream bases, same run starts, sequence indices and positions."""
+import os
+
+import numpy as np
+import pytest
+
+from golden_cases import GOLDEN
+from test_host_cpu import _oracle_stream
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_parse(scanner, raw: bytes):
+    torch = pytest.importorskip("torch")
+    n = len(raw)
+    d_raw = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
+    d_b = torch.empty(max(n, 1), dtype=torch.uint8, device="cuda")
+    d_rs, d_rq, d_rp, d_h = (torch.empty(max(n, 1), dtype=torch.int64, device="cuda") for _ in range(4))
+    nb, nr, ns = scanner.fasta_parse_device(d_raw.data_ptr(), n, d_b.data_ptr(), d_rs.data_ptr(), d_rq.data_ptr(),
+                                            d_rp.data_ptr(), d_h.data_ptr())
+    return (d_b[:nb].cpu().numpy(), d_rs[:nr].cpu().numpy(), d_rq[:nr].cpu().numpy(), d_rp[:nr].cpu().numpy(),
+            d_h[:ns].cpu().numpy())
+
+
+def _concat(files):
+    parts = []
+    for f in files:
+        b = open(f, "rb").read()
+        parts.append(b if b.endswith(b"\n") else b + b"\n")
+    return b"".join(parts)
+
+
+def _check(scanner, files):
+    raw = _concat(files)
+    got = _gpu_parse(scanner, raw)
+    want = _oracle_stream(files)
+    for name, g, w in zip(("bases", "run_start", "run_seq", "run_seqpos"), got[:4], want):
+        assert np.array_equal(g, w), f"{name}: {g[:8]} vs {w[:8]}"
+    hp = got[4]
+    assert all(raw[int(p)] == ord(">") for p in hp)
+    return got
+
+
+def test_golden_fasta_files(scanner):
+    files = [os.path.join(GOLDEN, "mixed", "seqs", f) for f in ("a_file.fa", "b_file.fa")]
+    _check(scanner, files)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_random_fasta_with_n_runs_lowercase_crlf_and_empty_lines(scanner, tmp_path, seed):
+    rng = np.random.default_rng(seed)
+    files = []
+    for fi in range(3):
+        lines = []
+        for si in range(int(rng.integers(1, 6))):
+            lines.append(f">seq{fi}_{si} some description")
+            L = int(rng.integers(0, 20_000))
+            s = rng.choice(np.frombuffer(b"ACGTACGTacgtNNnRY", dtype=np.uint8), size=L)
+            # N runs
+            for _ in range(int(rng.integers(0, 4))):
+                a = int(rng.integers(0, max(1, L)))
+                s[a:a + int(rng.integers(1, 500))] = ord("N")
+            w = int(rng.integers(1, 120))
+            eol = "\r\n" if rng.random() < 0.3 else "\n"
+            for k in range(0, L, w):
+                lines.append(s[k:k + w].tobytes().decode() + ("" if eol == "\n" else "\r"))
+                if rng.random() < 0.02:
+                    lines.append("")
+        p = tmp_path / f"f{fi}.fa"
+        p.write_bytes(("\n".join(lines) + "\n").encode())
+        files.append(str(p))
+    _check(scanner, files)
+
+
+def test_sequence_before_header_is_rejected(scanner):
+    from blamm_gb300 import BlammError
+    with pytest.raises(BlammError):
+        _gpu_parse(scanner, b"ACGT\n>s\nACGT\n")
