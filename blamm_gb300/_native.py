@@ -89,8 +89,9 @@ def gpu_lib() -> C.CDLL:
                                            vp, C.c_int, vp, vp]
     lib.blamm_device_memory.argtypes = [C.c_int, C.POINTER(i64), C.POINTER(i64)]
     lib.blamm_set_plan_options.argtypes = [vp, C.c_int, C.c_float]
+    lib.blamm_debug_stall.argtypes = [vp, C.c_int, C.c_longlong]
     lib.blamm_fasta_parse_device.argtypes = [vp, vp, i64, vp, C.POINTER(i64), vp, vp, vp, C.POINTER(i64), vp,
-                                             C.POINTER(i64)]
+                                             C.POINTER(i64), vp]
     lib.blamm_get_plan_options.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
@@ -99,7 +100,7 @@ def gpu_lib() -> C.CDLL:
                  "blamm_debug_profile_read", "blamm_scan_device_static", "blamm_set_columns",
                  "blamm_reserve", "blamm_scan_enqueue", "blamm_scan_graph_create", "blamm_scan_graph_launch",
                  "blamm_autotune", "blamm_theoretical_hist", "blamm_device_memory", "blamm_set_plan_options",
-                 "blamm_get_plan_options", "blamm_fasta_parse_device"):
+                 "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -248,13 +249,19 @@ class GpuScanner:
         return thr, cnt
 
     def fasta_parse_device(self, d_raw: int, nraw: int, d_bases: int, d_run_start: int, d_run_seq: int,
-                           d_run_seqpos: int, d_header_pos: int) -> tuple[int, int, int]:
-        """GPU FASTA ingest into caller device buffers: (bases, runs, sequences)."""
+                           d_run_seqpos: int, d_header_pos: int, nucl: np.ndarray | None = None) -> tuple[int, int, int]:
+        """GPU FASTA ingest into caller device buffers: (bases, runs, sequences); the stream's
+        A/C/G/T counts go to `nucl` (uint64[4]) when given."""
         nb, nr, ns = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self.lib.blamm_fasta_parse_device(
             self.h, C.c_void_p(d_raw), nraw, C.c_void_p(d_bases), C.byref(nb), C.c_void_p(d_run_start),
-            C.c_void_p(d_run_seq), C.c_void_p(d_run_seqpos), C.byref(nr), C.c_void_p(d_header_pos), C.byref(ns)))
+            C.c_void_p(d_run_seq), C.c_void_p(d_run_seqpos), C.byref(nr), C.c_void_p(d_header_pos), C.byref(ns),
+            _ptr(nucl) if nucl is not None else None))
         return nb.value, nr.value, ns.value
+
+    def debug_stall(self, enable: bool, wait_limit_cycles: int = 0) -> None:
+        """Failure-path test hook (see blamm_debug_stall)."""
+        self._check(self.lib.blamm_debug_stall(self.h, int(enable), wait_limit_cycles))
 
     def set_plan_options(self, max_tile_columns: int, job_cost: float) -> None:
         self._check(self.lib.blamm_set_plan_options(self.h, max_tile_columns, job_cost))

@@ -37,6 +37,7 @@ struct blamm_ctx {
     bool plain_timed = false, rescore_timed = false;
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
+    int debug_stall = 0;                  // test hook: make the scan kernel's first wait run out
 
     // motif bank (host copy); `active` lists the columns scanned (all when empty)
     int ncols = 0, p_rows = 0, lmax = 0;
@@ -582,6 +583,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         p.cand_cap = ctx->cand_cap;
         p.status = ctx->d_status;
         p.wait_limit = ctx->wait_limit;
+        p.debug_stall = ctx->debug_stall;
         p.dump = dump;
         p.dump_p0 = dump_p0;
         p.dump_npos = dump_npos;
@@ -909,6 +911,14 @@ int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const i
     cleanup();
     if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
     for (size_t i = 0; i < nc * (size_t)nbins; ++i) counts[i] += host[i];
+    return BLAMM_OK;
+}
+
+int blamm_debug_stall(blamm_ctx *ctx, int enable, long long wait_limit_cycles)
+{
+    if (!ctx || wait_limit_cycles < 0) return BLAMM_ERR_ARG;
+    ctx->debug_stall = enable ? 1 : 0;
+    ctx->wait_limit = wait_limit_cycles > 0 ? wait_limit_cycles : 4000000000LL;
     return BLAMM_OK;
 }
 
@@ -1557,10 +1567,12 @@ extern "C" {
 
 int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
                              int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
-                             int64_t *d_header_pos, int64_t *nseqs)
+                             int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts)
 {
     if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs) return BLAMM_ERR_ARG;
     *n_bases = *nruns = *nseqs = 0;
+    if (nucl_counts)
+        for (int b = 0; b < 4; ++b) nucl_counts[b] = 0;
     if (nraw == 0) return BLAMM_OK;
     if (!d_raw || !d_bases || !d_run_start || !d_run_seq || !d_run_seqpos || !d_header_pos)
         return fail(ctx, BLAMM_ERR_ARG, "null buffer");
@@ -1571,6 +1583,7 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     // the per-sequence character offsets, scan scratch and a status word
     int64_t *A = nullptr, *B = nullptr, *Cc = nullptr, *D = nullptr, *sc0 = nullptr, *scr = nullptr;
     int *bad = nullptr;
+    unsigned long long *nucl = nullptr;
     cudaError_t e = cudaMallocAsync(&A, 8 * n, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&B, 8 * n, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&Cc, 8 * n, st);
@@ -1579,6 +1592,8 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     if (e == cudaSuccess) e = cudaMallocAsync(&scr, 8 * sw, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&bad, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&nucl, 4 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nucl, 0, 4 * sizeof(unsigned long long), st);
     const unsigned grid = (unsigned)std::min<int64_t>((nraw + 255) / 256, (int64_t)ctx->sm_count * 32);
     if (e == cudaSuccess) {
         ingest_lines_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B);
@@ -1607,9 +1622,12 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bseq, 8 * (size_t)nb, st);
     if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bpos, 8 * (size_t)nb, st);
     if (e == cudaSuccess && !badh && nb > 0) {
-        ingest_bases_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B, Cc, D, sc0, d_bases, bseq, bpos);
+        ingest_bases_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B, Cc, D, sc0, d_bases, bseq, bpos, nucl);
         e = cudaGetLastError();
     }
+    unsigned long long nh[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess && !badh && nb > 0 && nucl_counts)
+        e = cudaMemcpyAsync(nh, nucl, sizeof nh, cudaMemcpyDeviceToHost, st);
     int64_t nr = 0;
     if (e == cudaSuccess && !badh && nb > 0) {
         // run flags into A (no longer needed), scanned in place
@@ -1623,7 +1641,7 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
         }
         if (e == cudaSuccess) e = cudaMemcpyAsync(&nr, A + nb - 1, 8, cudaMemcpyDeviceToHost, st);
     }
-    void *bufs[] = {A, B, Cc, D, sc0, scr, bad, bseq, bpos};
+    void *bufs[] = {A, B, Cc, D, sc0, scr, bad, bseq, bpos, nucl};
     for (void *b : bufs)
         if (b) cudaFreeAsync(b, st);
     const cudaError_t e2 = cudaStreamSynchronize(st);
@@ -1635,6 +1653,8 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     *n_bases = nb;
     *nruns = nr;
     *nseqs = ns;
+    if (nucl_counts)
+        for (int b = 0; b < 4; ++b) nucl_counts[b] = nh[b];
     return BLAMM_OK;
 }
 

@@ -131,18 +131,32 @@ __global__ void ingest_headers_kernel(const char *raw, int64_t n, const int64_t 
     }
 }
 
-// pass 3b: every stream base with its sequence and position in the sequence
+// pass 3b: every stream base with its sequence and position in the sequence, and the
+// A/C/G/T counts of the stream (Species::computeNucleotideComposition,
+// src/species.cpp:31-61: case-insensitive), one atomic per warp and base
 __global__ void ingest_bases_kernel(const char *raw, int64_t n, const int64_t *LS, const int64_t *HC,
                                     const int64_t *SC, const int64_t *VX, const int64_t *seq_sc0, char *bases,
-                                    int64_t *bseq, int64_t *bpos)
+                                    int64_t *bseq, int64_t *bpos, unsigned long long *nucl)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    for (int64_t i = start; i < n; i += stride) {
         const char c = raw[i];
         if (c == '\n' || raw[LS[i]] == '>' || !ingest_base((unsigned char)c)) continue;
         const int64_t o = VX[i] - 1, s = HC[i] - 1;
         bases[o] = c;
         bseq[o] = s;
         bpos[o] = SC[i] - 1 - seq_sc0[s];
+        const unsigned char u = (unsigned char)c;
+        ++cnt[((u >> 1) ^ (u >> 2)) & 3u];  // A/a=0 C/c=1 G/g=2 T/t=3
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        unsigned long long v = cnt[b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(nucl + b, v);
     }
 }
 

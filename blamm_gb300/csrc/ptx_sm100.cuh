@@ -72,6 +72,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
     }
 }
 
+// Bounded wait that ignores the abort flag: for copies and MMAs still in
+// flight after an abort, which must land before the CTA frees its shared and
+// tensor memory.
+__device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, long long limit_cycles)
+{
+    volatile int never = 0;
+    return mbar_wait(bar, parity, &never, limit_cycles);
+}
+
 // ---------------------------------------------------------------- fences
 __device__ __forceinline__ void fence_proxy_async_smem()
 {

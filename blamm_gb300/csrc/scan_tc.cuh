@@ -86,6 +86,7 @@ struct TcParams {
     int64_t cand_cap;
     int *status;         // bit 0: a device wait timed out
     long long wait_limit;  // clock64 cycles a wait may last
+    int32_t debug_stall;   // test hook: the MMA warp first waits on a barrier nobody completes
     // debug dump of the accumulator, sum(q) - T (positions [dump_p0, dump_p0+dump_npos))
     float *dump;
     int64_t dump_p0, dump_npos;
@@ -140,7 +141,8 @@ enum {
     BAR_BFULL = BAR_AEMPTY + kMaxAcc,    // B tile landed
     BAR_DRAIN = BAR_BFULL + 1,           // MMAs drained
     BAR_CODE = BAR_DRAIN + 1,            // code window landed   (kCodeStages)
-    BAR_COUNT = BAR_CODE + kCodeStages
+    BAR_NEVER = BAR_CODE + kCodeStages,  // never completed (the stall test hook)
+    BAR_COUNT = BAR_NEVER + 1
 };
 static_assert(BAR_COUNT <= 32, "the barrier area holds 32 mbarriers");
 
@@ -292,6 +294,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         ptx::mbar_init(bars + 8 * BAR_BFULL, 1);
         ptx::mbar_init(bars + 8 * BAR_DRAIN, 1);
         for (int s = 0; s < kCodeStages; ++s) ptx::mbar_init(bars + 8 * (BAR_CODE + s), 1);
+        ptx::mbar_init(bars + 8 * BAR_NEVER, 1);
         ptx::fence_mbar_init();
     }
     if (warp == kMmaWarp) {
@@ -317,7 +320,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const long long t_start = tick<kProf>();
             const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
             uint32_t jc = 0;
-            bool ok = true;
+            bool ok = true, b_pending = false;
+            if (p.debug_stall) ok = ptx::mbar_wait(bars + 8 * BAR_NEVER, 0, s_abort, p.wait_limit);
             JobIter it;
             for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
                 const int tile = it.tile;
@@ -336,9 +340,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     if (p.terms == 2)
                         ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes,
                                       (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
+                    b_pending = true;
                     ok = ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit);
-                    bphase ^= 1;
                     if (!ok) break;
+                    b_pending = false;
+                    bphase ^= 1;
                     cur_tile = tile;
                     if (kProf) t_b += tick<kProf>() - tb;
                     g_steps = (uint32_t)td.g;
@@ -377,9 +383,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
             }
-            // drain: nothing may still write TMEM when it is freed
+            // drain: nothing may still write TMEM or shared memory when they are freed
             ptx::mma_commit(bars + 8 * BAR_DRAIN);
-            if (!ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit)) *s_abort = 1;
+            if (!ptx::mbar_wait_drain(bars + 8 * BAR_DRAIN, dphase, p.wait_limit)) *s_abort = 1;
+            if (b_pending && !ptx::mbar_wait_drain(bars + 8 * BAR_BFULL, bphase, p.wait_limit)) *s_abort = 1;
             if (kProf) {
                 long long *pr = p.prof + 32 * blockIdx.x;
                 pr[0] = t_acc;
@@ -468,8 +475,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             for (uint32_t j = jc; j < jc + kCodeStages; ++j) {
                 const long long job = blockIdx.x + (long long)j * gridDim.x;
                 if (job >= njobs || *s_abort == 0) break;
-                ptx::mbar_wait(bars + 8 * (BAR_CODE + j % kCodeStages), (j / kCodeStages) & 1u, s_abort,
-                               p.wait_limit);
+                ptx::mbar_wait_drain(bars + 8 * (BAR_CODE + j % kCodeStages), (j / kCodeStages) & 1u,
+                                     p.wait_limit);
             }
     } else if (warp < kEpiWarps) {
         // ===================== epilogue (warps 0-15) ======================

@@ -190,11 +190,13 @@ int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols
  * bases (A/C/G/T/a/c/g/t), per run its stream start, sequence index and
  * position in the sequence (the SeqBlock markers, src/sequence.cpp:35-50),
  * and per sequence the byte offset of its '>' header line (names stay with
- * the caller).  Counts come back in *n_bases, *nruns, *nseqs.  Sequence data
- * before the first header gives BLAMM_ERR_ARG, as the reference rejects it. */
+ * the caller).  Counts come back in *n_bases, *nruns, *nseqs, and (optional,
+ * host memory) the A/C/G/T counts of the stream in nucl_counts[4] -- the
+ * dict module's nucleotide composition (src/species.cpp:31-61).  Sequence
+ * data before the first header gives BLAMM_ERR_ARG, as the reference rejects it. */
 int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
                              int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
-                             int64_t *d_header_pos, int64_t *nseqs);
+                             int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts);
 
 /* Number of CUDA devices (0 when there is no driver or device). */
 int blamm_device_count(int *n);
@@ -241,6 +243,13 @@ int blamm_guard_band(const blamm_ctx *ctx, float *out);
  * candidates, 16-23 drain of epilogue warps 0-7, 24-31 their waits).  *nctas
  * receives the CTA count. */
 int blamm_debug_profile(blamm_ctx *ctx, int enable);
+/* Failure-path test hook: with enable = 1 the tensor-core scan kernel first
+ * waits on a barrier that nothing completes; every wait of the kernel gives up
+ * after wait_limit_cycles (0 = the default, about 2 s of clock64 cycles), the
+ * CTAs drain their copies and MMAs, free their tensor memory and the call
+ * returns BLAMM_ERR_TIMEOUT; the context stays usable.  enable = 0 restores
+ * normal scans (with the given limit). */
+int blamm_debug_stall(blamm_ctx *ctx, int enable, long long wait_limit_cycles);
 int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, int *nctas);
 
 /* blamm_scan_device without allocation.  It has no counterpart in the

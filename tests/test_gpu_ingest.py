@@ -17,10 +17,11 @@ def _gpu_parse(scanner, raw: bytes):
     d_raw = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
     d_b = torch.empty(max(n, 1), dtype=torch.uint8, device="cuda")
     d_rs, d_rq, d_rp, d_h = (torch.empty(max(n, 1), dtype=torch.int64, device="cuda") for _ in range(4))
+    nucl = np.zeros(4, dtype=np.uint64)
     nb, nr, ns = scanner.fasta_parse_device(d_raw.data_ptr(), n, d_b.data_ptr(), d_rs.data_ptr(), d_rq.data_ptr(),
-                                            d_rp.data_ptr(), d_h.data_ptr())
+                                            d_rp.data_ptr(), d_h.data_ptr(), nucl)
     return (d_b[:nb].cpu().numpy(), d_rs[:nr].cpu().numpy(), d_rq[:nr].cpu().numpy(), d_rp[:nr].cpu().numpy(),
-            d_h[:ns].cpu().numpy())
+            d_h[:ns].cpu().numpy(), nucl)
 
 
 def _concat(files):
@@ -39,6 +40,9 @@ def _check(scanner, files):
         assert np.array_equal(g, w), f"{name}: {g[:8]} vs {w[:8]}"
     hp = got[4]
     assert all(raw[int(p)] == ord(">") for p in hp)
+    # the dict module's nucleotide composition of the stream
+    low = want[0] | 0x20
+    assert [int(x) for x in got[5]] == [int(np.count_nonzero(low == ord(c))) for c in "acgt"]
     return got
 
 
@@ -77,3 +81,13 @@ def test_sequence_before_header_is_rejected(scanner):
     from blamm_gb300 import BlammError
     with pytest.raises(BlammError):
         _gpu_parse(scanner, b"ACGT\n>s\nACGT\n")
+
+
+def test_nucleotide_counts_equal_the_reference_dictionary(scanner):
+    """The config-1 case's sequences.mf.dict (written by the reference's dict module) holds
+    NUCL_COUNT_ACGT of its FASTA file; the GPU ingest gives the same four counts."""
+    d = os.path.join(GOLDEN, "config1")
+    words = open(os.path.join(d, "expected", "sequences.mf.dict")).read().split()
+    want = [int(x) for x in words[words.index("NUCL_COUNT_ACGT") + 1:][:4]]
+    got = _gpu_parse(scanner, _concat([os.path.join(d, "seqs", "seqs.fa")]))
+    assert [int(x) for x in got[5]] == want

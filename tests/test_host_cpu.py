@@ -160,3 +160,14 @@ def test_bank_hist_columns_map_rc_columns_to_their_forward_motif():
         assert rc[h] == 0 and bank.name(h) == bank.name(c).replace("_rc", "")[: len(bank.name(h))]
         if rc[c] == 0:
             assert h == c
+
+
+def test_cli_rejects_sequence_data_before_a_header(tmp_path):
+    """A FASTA file whose first line is sequence data: the same message and exit code as the
+    reference's dict module (FastaBatch::getNextLine throws, blstools.cpp:93-101 exits 1)."""
+    import subprocess
+    (tmp_path / "bad.fa").write_text("ACGT\n>s1\nACGTACGT\n")
+    (tmp_path / "bad.mf").write_text("sp\tbad.fa\n")
+    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=tmp_path, capture_output=True)
+    assert r.returncode == 1
+    assert b"Input file does not appear to be in fasta format" in r.stderr + r.stdout
