@@ -539,6 +539,29 @@ static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
     return BLAMM_OK;
 }
 
+// Kernel parameters of the current plan over a packed stream of n positions
+// (the caller adds candidates, counters, status and the test hooks).
+static TcParams tc_params(const blamm_ctx *ctx, const uint32_t *seq2, const uint32_t *zmask, int64_t n)
+{
+    TcParams p{};
+    p.seq2 = seq2;
+    p.zmask = zmask;
+    p.n = n;
+    p.n_mtiles = (n + kBM - 1) / kBM;
+    p.tiles = ctx->d_tiles;
+    p.ntiles = (int32_t)ctx->tiles.size();
+    p.terms = ctx->plan_terms;
+    p.bbuf = ctx->d_bbuf;
+    p.slot_col = ctx->d_slot_col;
+    p.erows = ctx->erows;
+    p.b_term_max = ctx->b_term_max;
+    p.tmem_cols = ctx->tmem_cols;
+    p.acc_stages = ctx->acc_stages;
+    p.wait_limit = ctx->wait_limit;
+    p.dump_ncols = ctx->ncols;
+    return p;
+}
+
 // tcgen05 scan + rescoring; candidates buffer grows (and the scan re-runs) on overflow
 static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
                   int64_t hit_cap, float *dump, int64_t dump_p0, int64_t dump_npos, int *launches)
@@ -564,20 +587,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     for (int attempt = 0; attempt < 3; ++attempt) {
         CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-        TcParams p{};
-        p.seq2 = ctx->d_seq2;
-        p.zmask = ctx->d_zmask;
-        p.n = n;
-        p.n_mtiles = n_mtiles;
-        p.tiles = ctx->d_tiles;
-        p.ntiles = (int32_t)ctx->tiles.size();
-        p.terms = ctx->plan_terms;
-        p.bbuf = ctx->d_bbuf;
-        p.slot_col = ctx->d_slot_col;
-        p.erows = ctx->erows;
-        p.b_term_max = ctx->b_term_max;
-        p.tmem_cols = ctx->tmem_cols;
-        p.acc_stages = ctx->acc_stages;
+        TcParams p = tc_params(ctx, ctx->d_seq2, ctx->d_zmask, n);
         p.cand = ctx->d_cand;
         p.cand_count = ctx->d_counters;
         p.cand_cap = ctx->cand_cap;
@@ -1137,20 +1147,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         if ((int)L.total > ctx->max_smem)
             return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
         const uint32_t smem = std::max<uint32_t>(L.total, 116 * 1024);
-        TcParams p{};
-        p.seq2 = seq2;
-        p.zmask = zmask;
-        p.n = n;
-        p.n_mtiles = n_mtiles;
-        p.tiles = ctx->d_tiles;
-        p.ntiles = (int32_t)ctx->tiles.size();
-        p.terms = ctx->plan_terms;
-        p.bbuf = ctx->d_bbuf;
-        p.slot_col = ctx->d_slot_col;
-        p.erows = ctx->erows;
-        p.b_term_max = ctx->b_term_max;
-        p.tmem_cols = ctx->tmem_cols;
-        p.acc_stages = ctx->acc_stages;
+        TcParams p = tc_params(ctx, seq2, zmask, n);
         p.cand = cand;
         p.cand_count = counters;
         p.cand_cap = kStaticCandCap;
@@ -1295,20 +1292,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
-    TcParams p{};
-    p.seq2 = ctx->d_seq2;
-    p.zmask = ctx->d_zmask;
-    p.n = n;
-    p.n_mtiles = n_mtiles;
-    p.tiles = ctx->d_tiles;
-    p.ntiles = (int32_t)ctx->tiles.size();
-    p.terms = ctx->plan_terms;
-    p.bbuf = ctx->d_bbuf;
-    p.slot_col = ctx->d_slot_col;
-    p.erows = ctx->erows;
-    p.b_term_max = ctx->b_term_max;
-    p.tmem_cols = ctx->tmem_cols;
-    p.acc_stages = ctx->acc_stages;
+    TcParams p = tc_params(ctx, ctx->d_seq2, ctx->d_zmask, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
     p.cand_cap = ctx->cand_cap;

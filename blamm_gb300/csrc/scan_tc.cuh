@@ -157,6 +157,15 @@ __device__ __forceinline__ uint32_t and32(const uint32_t (&v)[32])
     return (a & b & c) & (t[9] & t[10]);
 }
 
+// Bit i set <=> word i is non-negative (sign bit clear), i.e. column i is a candidate.
+__device__ __forceinline__ uint32_t sign_mask(const uint32_t (&v)[32])
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int i = 31; i >= 0; --i) m = m * 2u + (v[i] >> 31);  // one shift and one multiply-add per bit
+    return ~m;
+}
+
 // The jobs of one CTA: job = blockIdx.x + k * gridDim.x, tile = job / n_mtiles,
 // m = job % n_mtiles, advanced without 64-bit divisions after the first.
 struct JobIter {
@@ -529,24 +538,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             }
             if (has_a) {
                 const long long tr0 = tick<kProf>();
-                const uint32_t r = has_b ? (and32(va) & and32(vb)) : and32(va);
-                const bool any = valid && (int32_t)r >= 0;
-                if (__any_sync(0xffffffffu, any)) {  // rare: stage this warp's candidates
+                // sign bit of the AND clear <=> some column of the chunk is a candidate
+                const bool any_a = valid && (int32_t)and32(va) >= 0;
+                const bool any_b = has_b && valid && (int32_t)and32(vb) >= 0;
+                if (__any_sync(0xffffffffu, any_a || any_b)) {  // rare: stage this warp's candidates
                     ++n_rare;
-                    uint32_t m0 = 0, m1 = 0;
-                    if (any) {
-#pragma unroll
-                        for (int i = 0; i < 32; ++i) {
-                            m0 |= ((~va[i]) >> 31) << i;
-                            m1 |= ((~vb[i]) >> 31) << i;
-                        }
-                        if (!has_b) m1 = 0u;
-                    }
-                    fill = stage_candidates(m0, slot0 + ca * 32, pos, lane, buf, fill, p.cand, p.cand_count,
-                                            p.cand_cap);
-                    if (has_b)
-                        fill = stage_candidates(m1, slot0 + cb * 32, pos, lane, buf, fill, p.cand, p.cand_count,
-                                                p.cand_cap);
+                    if (__any_sync(0xffffffffu, any_a))
+                        fill = stage_candidates(any_a ? sign_mask(va) : 0u, slot0 + ca * 32, pos, lane, buf, fill,
+                                                p.cand, p.cand_count, p.cand_cap);
+                    if (__any_sync(0xffffffffu, any_b))
+                        fill = stage_candidates(any_b ? sign_mask(vb) : 0u, slot0 + cb * 32, pos, lane, buf, fill,
+                                                p.cand, p.cand_count, p.cand_cap);
                 }
                 if (kDump && pos >= p.dump_p0 && pos < p.dump_p0 + p.dump_npos) {
                     // debug instantiation only: raw accumulator of some positions
