@@ -84,7 +84,7 @@ struct blamm_ctx {
     int *d_status = nullptr;
     bool prof_on = false;
     long long *d_prof = nullptr;
-    std::vector<long long> prof;  // last scan's role timing, 16 per CTA
+    std::vector<long long> prof;  // last scan's role timing, 32 counters per CTA
     int prof_ctas = 0;
 
     blamm_stats stats{};

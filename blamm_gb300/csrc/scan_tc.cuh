@@ -2,7 +2,7 @@
 // one persistent CTA per SM.
 //
 // Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
-// For an M tile of 128 positions starting at m0, the W-builder warp writes
+// For an M tile of 128 positions starting at m0, the E-builder warps write
 // one 16-byte entry per position, E[i] = onehot(base m0+i) ++ onehot(base
 // m0+i+1) (2 bases x 4 channels x bf16).  Read with row stride 16 B, 8-row
 // group stride (SBO) 128 B and K-core stride (LBO) 32 B, the entries starting
@@ -30,12 +30,14 @@
 // issues the MMAs and the TMA bulk copies of B tiles; warps 17-19 build E from
 // 2-bit code windows that one of their threads prefetches with TMA bulk copies
 // kCodeStages jobs ahead.  kEStages E stages and 2 or 4 TMEM accumulator stages (4 when
-// the plan's N tiles are at most 128 wide) keep the roles overlapped: the MMA warp may
-// run several jobs ahead of the drain.
+// the plan's N tiles are at most 128 wide) keep the roles overlapped.  A drain warp
+// hands its accumulator back right after its TMEM loads; the sign test and the
+// staging of candidates run on registers while the MMAs of the next job proceed.
 // Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
-// major, so a CTA reloads B only when its tile changes.  Every wait is
-// bounded: on a timeout the CTA raises an abort flag, every role stops,
-// outstanding MMAs are drained and TMEM is freed.
+// major, so a CTA reloads B only when its tile changes.  Every wait is an
+// mbarrier try-wait that sleeps and is bounded: on a timeout the CTA raises an
+// abort flag, every role stops, copies and MMAs in flight are drained, TMEM is
+// freed and the status word tells the host.
 #pragma once
 #include <cstdint>
 
@@ -96,10 +98,11 @@ struct TcParams {
 };
 
 // tc_prof_fields: 0 MMA wait acc_empty, 1 MMA wait E full, 2 MMA B reloads, 3 MMA loop,
-// 4 E wait code window, 5 E wait E empty, 6 E loop, 7 epilogue wait acc_full,
-// 8 epilogue loop, 9 epilogue drain (acc_full -> acc_empty arrive), 10 jobs,
-// 11 E-builder build time, 12 epilogue rounds with a candidate, 16-23 drain time of
-// epilogue warps 0-7, 24-31 their accumulator waits
+// 4 E wait code window, 5 E wait E empty, 6 epilogue hand-back (fence + arrive),
+// 7 epilogue wait acc_full, 8 epilogue loop, 9 epilogue drain (acc_full -> acc_empty
+// arrive), 10 jobs, 11 E-builder build time, 12 epilogue rounds with a candidate,
+// 13 epilogue TMEM loads, 14 epilogue fence after the wait, 15 epilogue sign test and
+// staging, 16-23 drain time of epilogue warps 0-7, 24-31 their accumulator waits
 
 // bytes of one prefetched code window (2-bit codes and zero mask) for erows entries
 __host__ __device__ inline uint32_t code_seq_bytes(int erows) { return (uint32_t)(((erows + 2 + 15) / 16 * 4 + 15) / 16 * 16); }
