@@ -234,6 +234,11 @@ int runScanModule(int argc, char **argv)
         std::cerr << "CUDA error: no devices found. Aborting..." << std::endl;
         return 1;
     }
+    if (o.mode != BLAMM_MODE_FP32 && motifs.maxMotifLen() > BLAMM_MAX_TC_MOTIF_LEN) {
+        std::cout << "Motifs longer than " << BLAMM_MAX_TC_MOTIF_LEN
+                  << " positions: using the plain FP32 GPU scan" << std::endl;
+        o.mode = BLAMM_MODE_FP32;
+    }
     std::vector<Device> devs((size_t)ndev);
     for (int d = 0; d < ndev; ++d) {
         const int rc = blamm_ctx_create(d, &devs[(size_t)d].ctx);

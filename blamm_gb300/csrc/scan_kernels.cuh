@@ -13,12 +13,14 @@
 #pragma once
 #include <cstdint>
 
+#include "blamm_gpu.h"
+
 #include "ptx_sm100.cuh"
 
 namespace blamm {
 
 constexpr int kStreamPad = 2048;   // padding bases after the stream end
-constexpr int kMaxMotifLen = 1024; // longest motif (the plain kernel reads up to 255 + L bases past a block)
+constexpr int kMaxMotifLen = BLAMM_MAX_MOTIF_LEN;  // the plain kernel reads up to 255 + L bases past a block
 constexpr int kColBits = 20;       // tensor-core candidate = pos << 20 | tile slot
 
 // ------------------------------------------------------------------------

@@ -41,13 +41,14 @@
 #pragma once
 #include <cstdint>
 
+#include "blamm_gpu.h"
 #include "ptx_sm100.cuh"
 #include "scan_kernels.cuh"
 
 namespace blamm {
 
 constexpr int kBM = 128;         // positions per M tile (= UMMA M)
-constexpr int kMaxTcLen = 256;   // longest motif on the tensor-core path
+constexpr int kMaxTcLen = BLAMM_MAX_TC_MOTIF_LEN;  // longest motif on the tensor-core path
 constexpr int kCandBuf = 128;    // per-warp staging of candidates in SMEM
 constexpr int kEpiWarps = 16;    // TMEM drain warps (4 per lane quarter)
 constexpr int kMmaWarp = 16;

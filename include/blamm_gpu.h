@@ -37,6 +37,11 @@ extern "C" {
 #define BLAMM_ERR_UNSUPPORTED (-6) /* e.g. no sm_100-class GPU, motif too long */
 #define BLAMM_ERR_STATE (-7)       /* call order (e.g. scan before set_motifs) */
 
+/* longest motifs: the tensor-core modes take motifs up to BLAMM_MAX_TC_MOTIF_LEN
+ * positions (longer ones need BLAMM_MODE_FP32); every mode up to BLAMM_MAX_MOTIF_LEN */
+#define BLAMM_MAX_TC_MOTIF_LEN 256
+#define BLAMM_MAX_MOTIF_LEN 1024
+
 /* arithmetic of the contraction (the emitted scores are FP32-exact in all modes) */
 #define BLAMM_MODE_FP32 0   /* plain SIMT FP32 sums: the straightforward GPU form */
 #define BLAMM_MODE_BF16 1   /* tcgen05, P as one BF16 term, wide guard band */
