@@ -357,6 +357,8 @@ def host_lib() -> C.CDLL:
     lib.blamm_bank_matrix.argtypes = [vp, vp, vp, vp]
     lib.blamm_bank_min_max.argtypes = [vp, vp, vp]
     lib.blamm_bank_pvalue_thresholds.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, vp]
+    lib.blamm_format_scores.argtypes = [vp, C.c_int64, C.c_char_p, C.c_int]
+    lib.blamm_format_scores.restype = C.c_int
     lib.blamm_bank_hist_columns.argtypes = [vp, vp]
     lib.blamm_bank_hist_columns.restype = C.c_int
     lib.blamm_bank_name.argtypes = [vp, C.c_int]
@@ -382,6 +384,16 @@ def host_lib() -> C.CDLL:
         getattr(lib, name).restype = C.c_int
     _host = lib
     return lib
+
+
+def format_scores(values: np.ndarray) -> list[bytes]:
+    """Scores as the occurrence file prints them (the host library's formatter)."""
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    out = C.create_string_buffer(32 * len(v))
+    if host_lib().blamm_format_scores(_ptr(v), len(v), out, 32) != 0:
+        raise BlammError(-1, "blamm_format_scores failed")
+    raw = out.raw
+    return [raw[32 * i:32 * i + 32].split(b"\0", 1)[0] for i in range(len(v))]
 
 
 class ServerConfig(C.Structure):

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "blamm_host.h"
+#include "format.h"
 #include "histogram.h"
 #include "motif.h"
 #include "sequence.h"
@@ -168,6 +169,13 @@ int blamm_bank_hist_columns(const blamm_bank *bank, int32_t *hist_of)
             hist_of[c] = it->second;
         }
     });
+}
+
+int blamm_format_scores(const float *values, int64_t n, char *out, int stride)
+{
+    if ((n > 0 && (!values || !out)) || n < 0 || stride < 16) return -1;
+    for (int64_t i = 0; i < n; ++i) blamm::formatScore(values[i], out + i * stride);
+    return 0;
 }
 
 const char *blamm_bank_name(const blamm_bank *bank, int c)

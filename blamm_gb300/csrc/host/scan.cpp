@@ -9,6 +9,7 @@
 // and writes the lines.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -24,6 +25,7 @@
 #include <vector>
 
 #include "blamm_gpu.h"
+#include "format.h"
 #include "histogram.h"
 #include "motif.h"
 #include "sequence.h"
@@ -96,26 +98,77 @@ void scanChunk(Device &dev, const StreamChunk &chunk)
     }
 }
 
+using Clock = std::chrono::steady_clock;
+
+// Wall time per pipeline phase (summed over threads), printed to stderr when the
+// environment sets BLAMM_TIMING.
+struct PhaseTiming {
+    std::mutex mu;
+    double s[5] = {0, 0, 0, 0, 0};
+    void add(int k, Clock::duration d)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        s[k] += std::chrono::duration<double>(d).count();
+    }
+    void report()
+    {
+        std::fprintf(stderr, "timing: GPU scan calls %.3f s, ordering hits %.3f s, formatting %.3f s, "
+                             "FASTA reading %.3f s, writing %.3f s\n", s[0], s[1], s[2], s[3], s[4]);
+    }
+};
+PhaseTiming timing;
+
+// The hits of positions below `payload`, sorted by (position, column): a counting sort
+// on position blocks, then small sorts inside each block, blocks split over threads.
+std::vector<blamm_hit> orderHits(const std::vector<blamm_hit> &in, int64_t payload, size_t threads)
+{
+    const int64_t kBlock = 4096;
+    const int64_t nb = std::max<int64_t>(1, (payload + kBlock - 1) / kBlock);
+    std::vector<int64_t> start((size_t)nb + 1, 0);
+    for (const blamm_hit &x : in)
+        if (x.pos < payload) ++start[(size_t)(x.pos / kBlock) + 1];
+    for (int64_t b = 0; b < nb; ++b) start[(size_t)b + 1] += start[(size_t)b];
+    std::vector<blamm_hit> out((size_t)start[(size_t)nb]);
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (const blamm_hit &x : in)
+        if (x.pos < payload) out[(size_t)fill[(size_t)(x.pos / kBlock)]++] = x;
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(threads, out.size() / 100000 + 1));
+    auto sortBlocks = [&](int64_t b0, int64_t b1) {
+        for (int64_t b = b0; b < b1; ++b)
+            std::sort(out.begin() + start[(size_t)b], out.begin() + start[(size_t)b + 1],
+                      [](const blamm_hit &a, const blamm_hit &c) { return a.pos != c.pos ? a.pos < c.pos : a.col < c.col; });
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t) th.emplace_back(sortBlocks, nb * (int64_t)t / (int64_t)nt, nb * (int64_t)(t + 1) / (int64_t)nt);
+    for (auto &x : th) x.join();
+    return out;
+}
+
 // format "seq\tblamm\tmotif\tstart\tend\tscore\tstrand\t.\t." lines (pwmscan.cpp:88-95);
 // floats as the reference's default ostream (%g, 6 significant digits)
 void formatHits(const std::vector<blamm_hit> &hits, size_t lo, size_t hi, const StreamChunk &chunk,
                 const Species &species, const MotifContainer &motifs, std::string &out)
 {
-    char buf[64];
+    static const std::string kNone;
+    char buf[96];
     for (size_t i = lo; i < hi; ++i) {
         const blamm_hit &h = hits[i];
         const Marker m = chunk.locate(h.pos);
         const Motif &mo = motifs[(size_t)h.col];
-        const std::string &seqName = (size_t)m.seqIdx < species.seqNames().size()
-                                         ? species.seqName((size_t)m.seqIdx)
-                                         : std::string();
+        const std::string &seqName =
+            (size_t)m.seqIdx < species.seqNames().size() ? species.seqName((size_t)m.seqIdx) : kNone;
         out += seqName;
         out += "\tblamm\t";
         out += mo.name();
-        int k = snprintf(buf, sizeof buf, "\t%lld\t%lld\t%g\t%c\t.\t.\n", (long long)m.seqPos,
-                         (long long)(m.seqPos + (int64_t)mo.size()), (double)h.score,
-                         mo.isRevCompl() ? '-' : '+');
-        out.append(buf, (size_t)k);
+        int k = 0;
+        buf[k++] = '\t';
+        k += formatUnsigned((uint64_t)m.seqPos, buf + k);
+        buf[k++] = '\t';
+        k += formatUnsigned((uint64_t)(m.seqPos + (int64_t)mo.size()), buf + k);
+        buf[k++] = '\t';
+        k += formatScore(h.score, buf + k);
+        std::memcpy(buf + k, mo.isRevCompl() ? "\t-\t.\t.\n" : "\t+\t.\t.\n", 7);
+        out.append(buf, (size_t)k + 7);
     }
 }
 
@@ -306,7 +359,10 @@ int runScanModule(int argc, char **argv)
                         if (failure) break;
                     }
                     auto chunk = std::make_shared<StreamChunk>();
-                    if (!fs.nextChunk(*chunk, payload, overlap)) break;
+                    const auto t0 = Clock::now();
+                    const bool more = fs.nextChunk(*chunk, payload, overlap);
+                    timing.add(3, Clock::now() - t0);
+                    if (!more) break;
                     std::lock_guard<std::mutex> lk(mu);
                     todo.emplace_back(nextRead++, chunk);
                     cv.notify_all();
@@ -332,15 +388,13 @@ int runScanModule(int argc, char **argv)
                         cv.notify_all();
                     }
                     const StreamChunk &chunk = *job.second;
+                    const auto t0 = Clock::now();
                     scanChunk(dev, chunk);
-                    // keep the chunk's own positions (the overlap belongs to the next chunk)
-                    auto &h = dev.hits;
-                    h.erase(std::remove_if(h.begin(), h.end(),
-                                           [&](const blamm_hit &x) { return x.pos >= chunk.payload; }),
-                            h.end());
-                    std::sort(h.begin(), h.end(), [](const blamm_hit &a, const blamm_hit &b) {
-                        return a.pos != b.pos ? a.pos < b.pos : a.col < b.col;
-                    });
+                    const auto t1 = Clock::now();
+                    // the chunk's own positions (the overlap belongs to the next chunk), in
+                    // stream order
+                    std::vector<blamm_hit> h = orderHits(dev.hits, chunk.payload, o.numThreads);
+                    const auto t2 = Clock::now();
                     // format in parallel slices
                     const size_t nt = std::max<size_t>(1, std::min<size_t>(o.numThreads, h.size() / 20000 + 1));
                     std::vector<std::string> parts(nt);
@@ -351,7 +405,14 @@ int runScanModule(int argc, char **argv)
                         });
                     for (auto &x : th) x.join();
                     std::string text;
+                    size_t tl = 0;
+                    for (auto &p : parts) tl += p.size();
+                    text.reserve(tl);
                     for (auto &p : parts) text += p;
+                    const auto t3 = Clock::now();
+                    timing.add(0, t1 - t0);
+                    timing.add(1, t2 - t1);
+                    timing.add(2, t3 - t2);
                     std::unique_lock<std::mutex> lk(mu);
                     totMatches += h.size();
                     done.emplace(job.first, std::move(text));
@@ -384,7 +445,9 @@ int runScanModule(int argc, char **argv)
                 done.erase(it);
                 ++nextWrite;
             }
+            const auto t0 = Clock::now();
             os << text;
+            timing.add(4, Clock::now() - t0);
         }
         {
             std::lock_guard<std::mutex> lk(mu);
@@ -400,6 +463,7 @@ int runScanModule(int argc, char **argv)
     ofsCutoff.close();
     for (auto &d : devs) blamm_ctx_destroy(d.ctx);
     std::cout << "\nWrote " << totMatches << " matches to " << o.output << ".\n";
+    if (std::getenv("BLAMM_TIMING")) timing.report();
     return 0;
 }
 

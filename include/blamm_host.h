@@ -59,6 +59,11 @@ int blamm_bank_pvalue_thresholds(const blamm_bank *bank, const float bg_prob[4],
  * hist_of argument of blamm_theoretical_hist. */
 int blamm_bank_hist_columns(const blamm_bank *bank, int32_t *hist_of);
 
+/* Scores as the occurrence file prints them (the reference's default ostream
+ * output, printf %g: 6 significant digits): value i goes to out + i * stride as a
+ * zero-terminated string (stride >= 16). */
+int blamm_format_scores(const float *values, int64_t n, char *out, int stride);
+
 /* Name of column c (valid until the bank is freed). */
 const char *blamm_bank_name(const blamm_bank *bank, int c);
 

@@ -671,3 +671,8 @@ int64_t orc_scan_blas(const char *bases, int64_t n, const int64_t *run_start,
     free(sj); free(jobs); free(th); free(code);
     return tot;
 }
+
+void orc_format_scores(const float *values, int64_t n, char *out, int stride)
+{
+    for (int64_t i = 0; i < n; i++) snprintf(out + i * stride, (size_t)stride, "%g", (double)values[i]);
+}

@@ -117,6 +117,11 @@ int64_t orc_scan_blas(const char *bases, int64_t n, const int64_t *run_start,
 int orc_matrix_tiles(const int32_t *lens, int ncols, int64_t min_zero_area,
                      int32_t *tiles, int max_tiles);
 
+/* Scores as PWMScan::writeOccToDisk prints them (src/pwmscan.cpp:88-95): the
+ * default std::ostream float output, i.e. printf("%g"); value i goes to
+ * out + i * stride. */
+void orc_format_scores(const float *values, int64_t n, char *out, int stride);
+
 #ifdef __cplusplus
 }
 #endif

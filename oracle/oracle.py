@@ -171,3 +171,15 @@ def scan_blas(bases: np.ndarray, run_start: np.ndarray, P: np.ndarray, col_len, 
 
 def sort_hits(h: np.ndarray) -> np.ndarray:
     return np.sort(h, order=["pos", "col"])
+
+
+def format_scores(values: np.ndarray) -> list[bytes]:
+    """printf("%g") of each float (the reference's occurrence-file score text)."""
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    out = C.create_string_buffer(32 * len(v))
+    f = lib().orc_format_scores
+    f.argtypes = [C.c_void_p, C.c_int64, C.c_char_p, C.c_int]
+    f.restype = None
+    f(_p(v), len(v), out, 32)
+    raw = out.raw
+    return [raw[32 * i:32 * i + 32].split(b"\0", 1)[0] for i in range(len(v))]

@@ -171,3 +171,24 @@ def test_cli_rejects_sequence_data_before_a_header(tmp_path):
     r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=tmp_path, capture_output=True)
     assert r.returncode == 1
     assert b"Input file does not appear to be in fasta format" in r.stderr + r.stdout
+
+
+def test_score_text_equals_printf_g():
+    """The occurrence-file score formatter against printf("%g") (the reference's default
+    ostream output): a whole binade exhaustively, random magnitudes and signs, decimal
+    ties, carries to the next power of ten, and the values outside the fast path."""
+    from blamm_gb300._native import format_scores
+    rng = np.random.default_rng(7)
+    binade = (np.arange(1 << 23, dtype=np.uint32) | np.uint32(0x3F800000)).view(np.float32)  # [1, 2)
+    rand_mag = (np.exp(rng.uniform(np.log(1e-7), np.log(1e9), 2_000_000)) *
+                rng.choice([-1.0, 1.0], 2_000_000)).astype(np.float32)
+    scores = rng.uniform(-60, 40, 1_000_000).astype(np.float32)
+    ties = np.array([float(f"{d}.{x:05d}5") for d in range(1, 10) for x in range(0, 100000, 997)],
+                    dtype=np.float32)
+    edges = np.array([9.999995, 99999.95, 999999.5, 1e-4, 9.99999e-5, 1e6, 0.0, -0.0, 123456.5, 0.5,
+                      np.inf, -np.inf, np.nan, 1e-40, 3.4e38], dtype=np.float32)
+    for v in (binade, rand_mag, scores, ties, edges):
+        got = format_scores(v)
+        want = oracle.format_scores(v)
+        bad = [i for i, (g, w) in enumerate(zip(got, want)) if g != w]
+        assert not bad, [(float(v[i]), got[i], want[i]) for i in bad[:5]]
