@@ -580,6 +580,10 @@ static TcParams tc_params(const blamm_ctx *ctx, const uint32_t *seq2, const uint
     p.b_term_max = ctx->b_term_max;
     p.tmem_cols = ctx->tmem_cols;
     p.acc_stages = ctx->acc_stages;
+    // With two terms a job's MMAs take long enough that taking the accumulator wait off
+    // the issuing thread pays (5 % on a 40 Mbp stream x 1024 columns); with one term the
+    // extra hop of the relay costs more than it saves (6 %).
+    p.relay = ctx->plan_terms == 2;
     p.wait_limit = ctx->wait_limit;
     p.dump_ncols = ctx->ncols;
     return p;

@@ -33,6 +33,10 @@
 // the plan's N tiles are at most 128 wide) keep the roles overlapped.  A drain warp
 // hands its accumulator back right after its TMEM loads; the sign test and the
 // staging of candidates run on registers while the MMAs of the next job proceed.
+// Relayed hand-off (TcParams::relay): the issuing thread waits on one barrier
+// per job and commits once.  The E builders' first thread waits for the job's
+// accumulator to be free before it signals E full, and a drain thread signals
+// E empty once the job's MMAs are complete.
 // Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
 // major, so a CTA reloads B only when its tile changes.  Every wait is an
 // mbarrier try-wait that sleeps and is bounded: on a timeout the CTA raises an
@@ -84,6 +88,7 @@ struct TcParams {
     uint32_t b_term_max; // bytes reserved per B term in SMEM
     uint32_t tmem_cols;  // TMEM columns allocated (acc_stages accumulators)
     int32_t acc_stages;  // 2 (N <= 256) or 4 (N <= 128)
+    int32_t relay;       // 1: accumulator hand-back relayed through the E builders (see the roles)
     unsigned long long *cand;
     unsigned long long *cand_count;
     int64_t cand_cap;
@@ -369,7 +374,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;     // accumulator
                 const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
                 const long long t0 = tick<kProf>();
-                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
+                // relayed: E full already implies that the accumulator is free
+                ok = p.relay || ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
                 const long long t1 = tick<kProf>();
                 ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
                 if (kProf) {
@@ -393,7 +399,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     for (uint32_t g = 0; g < g_steps; ++g)
                         ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
                 }
-                ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
+                if (!p.relay) ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));  // relayed: by the drain
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
             }
             // drain: nothing may still write TMEM or shared memory when they are freed
@@ -430,6 +436,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         if (et == 0)
             for (uint32_t j = 0; j < kCodeStages; ++j) fetch(j);
         long long t_code = 0, t_we = 0, t_build = 0;
+        bool relay_fail = false;  // et 0 gave up waiting for a free accumulator
         const long long t_start = tick<kProf>();
         uint32_t jc = 0;
         JobIter it;
@@ -445,7 +452,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
             // every builder thread leaves together when any of them gave up (no one is left
             // waiting at the barrier below)
-            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok)) break;
+            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok || relay_fail)) break;
             if (kProf) {
                 t_code += t1 - t0;
                 t_we += tick<kProf>() - t1;
@@ -474,7 +481,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             if (kProf) t_build += tick<kProf>() - t2;
             if (et == 0) {
                 fetch(jc + kCodeStages);
-                ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
+                if (p.relay) {  // E full is signalled only once the job's accumulator is free
+                    const uint32_t as = jc & acc_mask, aph = (jc >> acc_shift) & 1u;
+                    relay_fail = !ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + as), aph ^ 1u, s_abort, p.wait_limit);
+                }
+                if (!relay_fail) ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
             }
         }
         if (kProf && et == 0) {
@@ -508,6 +519,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
             if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
+            // relayed: the job's MMAs are complete, so its E stage is free
+            if (p.relay && warp == 0 && lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WEMPTY + jc % kEStages));
             const long long t1 = tick<kProf>();
             if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
