@@ -400,8 +400,12 @@ int blamm_ctx_create(int device, blamm_ctx **out)
         ctx->max_smem = (int)prop.sharedMemPerBlockOptin;
         cudaFuncAttributes fa;
         // fails if no sm_103a image fits
-        for (const void *k : {(const void *)scan_tc_kernel<false, false>, (const void *)scan_tc_kernel<true, false>,
-                              (const void *)scan_tc_kernel<false, true>}) {
+        for (const void *k : {(const void *)scan_tc_kernel<false, false, 1>,
+                              (const void *)scan_tc_kernel<false, false, 2>,
+                              (const void *)scan_tc_kernel<true, false, 1>,
+                              (const void *)scan_tc_kernel<true, false, 2>,
+                              (const void *)scan_tc_kernel<false, true, 1>,
+                              (const void *)scan_tc_kernel<false, true, 2>}) {
             CK(cudaFuncGetAttributes(&fa, k));
             if (fa.maxThreadsPerBlock < kTcThreads)
                 return fail(ctx, BLAMM_ERR_UNSUPPORTED,
@@ -580,13 +584,24 @@ static TcParams tc_params(const blamm_ctx *ctx, const uint32_t *seq2, const uint
     p.b_term_max = ctx->b_term_max;
     p.tmem_cols = ctx->tmem_cols;
     p.acc_stages = ctx->acc_stages;
-    // With two terms a job's MMAs take long enough that taking the accumulator wait off
-    // the issuing thread pays (5 % on a 40 Mbp stream x 1024 columns); with one term the
-    // extra hop of the relay costs more than it saves (6 %).
-    p.relay = ctx->plan_terms == 2;
     p.wait_limit = ctx->wait_limit;
     p.dump_ncols = ctx->ncols;
     return p;
+}
+
+// One launch of the scan kernel instance that p asks for.
+template <bool kDump, bool kProf>
+static void launch_tc_as(const TcParams &p, int grid, uint32_t smem, cudaStream_t st)
+{
+    if (p.terms == 2) scan_tc_kernel<kDump, kProf, 2><<<grid, kTcThreads, smem, st>>>(p);
+    else scan_tc_kernel<kDump, kProf, 1><<<grid, kTcThreads, smem, st>>>(p);
+}
+
+static void launch_tc(const TcParams &p, bool dump, int grid, uint32_t smem, cudaStream_t st)
+{
+    if (dump) launch_tc_as<true, false>(p, grid, smem, st);
+    else if (p.prof) launch_tc_as<false, true>(p, grid, smem, st);
+    else launch_tc_as<false, false>(p, grid, smem, st);
 }
 
 // tcgen05 scan + rescoring; candidates buffer grows (and the scan re-runs) on overflow
@@ -634,9 +649,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
         if (njobs > 0) {
             CK(cudaEventRecord(ctx->ev[4], ctx->stream));
-            if (dump) scan_tc_kernel<true, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
-            else if (p.prof) scan_tc_kernel<false, true><<<grid, kTcThreads, smem, ctx->stream>>>(p);
-            else scan_tc_kernel<false, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+            launch_tc(p, dump != nullptr, grid, smem, ctx->stream);
             CK(cudaGetLastError());
             CK(cudaEventRecord(ctx->ev[5], ctx->stream));
             ++*launches;
@@ -1182,7 +1195,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.wait_limit = ctx->wait_limit;
         p.dump_ncols = ctx->ncols;
         const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-        scan_tc_kernel<false, false><<<grid, kTcThreads, smem, ctx->stream>>>(p);
+        launch_tc(p, false, grid, smem, ctx->stream);
         CK(cudaGetLastError());
         ++launches;
         unsigned long long ncand = 0;
@@ -1327,7 +1340,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     p.wait_limit = ctx->wait_limit;
     p.dump_ncols = ctx->ncols;
     const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-    scan_tc_kernel<false, false><<<grid, kTcThreads, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream>>>(p);
+    launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
     CK(cudaGetLastError());
     RescoreParams r{};
     r.cand = ctx->d_cand;

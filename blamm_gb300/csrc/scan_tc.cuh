@@ -33,10 +33,11 @@
 // the plan's N tiles are at most 128 wide) keep the roles overlapped.  A drain warp
 // hands its accumulator back right after its TMEM loads; the sign test and the
 // staging of candidates run on registers while the MMAs of the next job proceed.
-// Relayed hand-off (TcParams::relay): the issuing thread waits on one barrier
-// per job and commits once.  The E builders' first thread waits for the job's
-// accumulator to be free before it signals E full, and a drain thread signals
-// E empty once the job's MMAs are complete.
+// Start-signal hand-off (two-term instances): the issuing thread waits on one
+// barrier per job and commits once.  The accumulator stage's empty barrier
+// then counts the drain warps and the E builders' first thread, so that its
+// phase completes when the stage is drained AND the job's E stage is built;
+// a drain thread signals E empty once the job's MMAs are complete.
 // Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
 // major, so a CTA reloads B only when its tile changes.  Every wait is an
 // mbarrier try-wait that sleeps and is bounded: on a timeout the CTA raises an
@@ -88,7 +89,6 @@ struct TcParams {
     uint32_t b_term_max; // bytes reserved per B term in SMEM
     uint32_t tmem_cols;  // TMEM columns allocated (acc_stages accumulators)
     int32_t acc_stages;  // 2 (N <= 256) or 4 (N <= 128)
-    int32_t relay;       // 1: accumulator hand-back relayed through the E builders (see the roles)
     unsigned long long *cand;
     unsigned long long *cand_count;
     int64_t cand_cap;
@@ -271,13 +271,20 @@ __device__ __forceinline__ long long tick()
 }
 
 // kDump: also write the raw accumulator of some positions (test hook);
-// kProf: role timing into p.prof.  The scan itself is <false, false>.
-template <bool kDump, bool kProf>
+// kProf: role timing into p.prof; kTerms: p.terms (1 or 2).  The scan itself
+// is <false, false, p.terms>.  The issuing thread runs once per MMA and per
+// job, so every branch taken out of its loop at compile time shows in the scan
+// time (runtime mode switches cost 2-4 %).
+template <bool kDump, bool kProf, int kTerms>
 __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = smem_raw + ((1024 - (ptx::smem_addr(smem_raw) & 1023)) & 1023);
-    const TcSmem L = tc_smem_layout(p.b_term_max, p.terms, p.erows, p.ntiles);
+    // two terms: a job's MMAs take long enough that one start signal per job pays (7.5 %
+    // on a 40 Mbp stream x 1024 columns); with one term the E builders, which then may
+    // run only as far ahead as the accumulator stages, fall behind (6 % slower)
+    constexpr bool kStartSignal = kTerms == 2;
+    const TcSmem L = tc_smem_layout(p.b_term_max, kTerms, p.erows, p.ntiles);
     const uint32_t sbase = ptx::smem_addr(smem);
     unsigned long long *s_cand = reinterpret_cast<unsigned long long *>(smem + L.cand);
     TileDesc *s_tiles = reinterpret_cast<TileDesc *>(smem + L.tiles);
@@ -307,7 +314,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         }
         for (int s = 0; s < kMaxAcc; ++s) {
             ptx::mbar_init(bars + 8 * (BAR_AFULL + s), 1);
-            ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps);
+            // start-signal hand-off: the E builders arrive too; the drain warps' share of
+            // the first phase (no earlier job to drain) is pre-arrived
+            ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps + (kStartSignal ? 1 : 0));
+            if (kStartSignal)
+                for (int k = 0; k < kEpiWarps; ++k) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
         }
         ptx::mbar_init(bars + 8 * BAR_BFULL, 1);
         ptx::mbar_init(bars + 8 * BAR_DRAIN, 1);
@@ -352,10 +363,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                         if (!ok) break;
                     }
                     const TileDesc td = s_tiles[tile];
-                    ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * p.terms);
+                    ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * kTerms);
                     ptx::bulk_g2s(sbase + L.b_hi, p.bbuf + td.b_off, (uint32_t)td.b_bytes,
                                   bars + 8 * BAR_BFULL);
-                    if (p.terms == 2)
+                    if (kTerms == 2)
                         ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes,
                                       (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
                     b_pending = true;
@@ -374,10 +385,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;     // accumulator
                 const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
                 const long long t0 = tick<kProf>();
-                // relayed: E full already implies that the accumulator is free
-                ok = p.relay || ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
+                // start signal: phase ph of the stage's empty barrier (drained and E built);
+                // otherwise the previous phase (drained) and then E full
+                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), kStartSignal ? ph : ph ^ 1u, s_abort, p.wait_limit);
                 const long long t1 = tick<kProf>();
-                ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
+                ok = ok && (kStartSignal || ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit));
                 if (kProf) {
                     t_acc += t1 - t0;
                     t_w += tick<kProf>() - t1;
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 const uint64_t adesc0 = ptx::smem_desc(sbase + L.e0 + es * (uint32_t)p.erows * 16u, 32u, 128u);
                 // D = -T (bias pieces in the last k-step of the hi term)
                 ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
-                if (p.terms == 2) {
+                if (kTerms == 2) {
                     for (uint32_t g = 0; g < g_steps; ++g) {
                         ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
                         ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
@@ -399,7 +411,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     for (uint32_t g = 0; g < g_steps; ++g)
                         ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
                 }
-                if (!p.relay) ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));  // relayed: by the drain
+                if (!kStartSignal) ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));  // else by a drain thread
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
             }
             // drain: nothing may still write TMEM or shared memory when they are freed
@@ -436,7 +448,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         if (et == 0)
             for (uint32_t j = 0; j < kCodeStages; ++j) fetch(j);
         long long t_code = 0, t_we = 0, t_build = 0;
-        bool relay_fail = false;  // et 0 gave up waiting for a free accumulator
+        bool signal_fail = false;  // et 0 gave up waiting for the previous start signal
         const long long t_start = tick<kProf>();
         uint32_t jc = 0;
         JobIter it;
@@ -452,7 +464,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
             // every builder thread leaves together when any of them gave up (no one is left
             // waiting at the barrier below)
-            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok || relay_fail)) break;
+            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok || signal_fail)) break;
             if (kProf) {
                 t_code += t1 - t0;
                 t_we += tick<kProf>() - t1;
@@ -481,11 +493,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             if (kProf) t_build += tick<kProf>() - t2;
             if (et == 0) {
                 fetch(jc + kCodeStages);
-                if (p.relay) {  // E full is signalled only once the job's accumulator is free
+                if (kStartSignal) {
+                    // this arrival counts toward the job's start signal, so the stage's
+                    // previous start signal (its previous job) must have completed first
                     const uint32_t as = jc & acc_mask, aph = (jc >> acc_shift) & 1u;
-                    relay_fail = !ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + as), aph ^ 1u, s_abort, p.wait_limit);
+                    if (jc >= (uint32_t)p.acc_stages)
+                        signal_fail = !ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + as), aph ^ 1u, s_abort, p.wait_limit);
+                    if (!signal_fail) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + as));
+                } else {
+                    ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
                 }
-                if (!relay_fail) ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
             }
         }
         if (kProf && et == 0) {
@@ -519,8 +536,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
             if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
-            // relayed: the job's MMAs are complete, so its E stage is free
-            if (p.relay && warp == 0 && lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WEMPTY + jc % kEStages));
+            // start-signal hand-off: the job's MMAs are complete, so its E stage is free
+            if (kStartSignal && warp == 0 && lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WEMPTY + jc % kEStages));
             const long long t1 = tick<kProf>();
             if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
