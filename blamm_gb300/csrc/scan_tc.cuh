@@ -26,7 +26,7 @@
 // in exact FP32 (rescore_kernel).
 //
 // Roles (640 threads): warps 0-15 drain TMEM (lane quarter = warp % 4, column
-// group = warp / 4) and test sign bits; warp 16 allocates TMEM and one lane
+// group = warp / 4) and test for candidates; warp 16 allocates TMEM and one lane
 // issues the MMAs and the TMA bulk copies of B tiles; warps 17-19 build E from
 // 2-bit code windows that one of their threads prefetches with TMA bulk copies
 // kCodeStages jobs ahead.  kEStages E stages and 2 or 4 TMEM accumulator stages (4 when
@@ -155,24 +155,19 @@ enum {
 };
 static_assert(BAR_COUNT <= 32, "the barrier area holds 32 mbarriers");
 
-// AND of 32 words as a shallow tree (3-input LOPs)
-__device__ __forceinline__ uint32_t and32(const uint32_t (&v)[32])
-{
-    uint32_t t[11];
-#pragma unroll
-    for (int i = 0; i < 10; ++i) t[i] = v[3 * i] & v[3 * i + 1] & v[3 * i + 2];
-    t[10] = v[30] & v[31];
-    const uint32_t a = t[0] & t[1] & t[2], b = t[3] & t[4] & t[5], c = t[6] & t[7] & t[8];
-    return (a & b & c) & (t[9] & t[10]);
-}
-
 // Bit i set <=> word i is non-negative (sign bit clear), i.e. column i is a candidate.
+// One funnel shift per word ((m << 1) | (v >> 31)), in four independent chains.
 __device__ __forceinline__ uint32_t sign_mask(const uint32_t (&v)[32])
 {
-    uint32_t m = 0;
+    uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
 #pragma unroll
-    for (int i = 31; i >= 0; --i) m = m * 2u + (v[i] >> 31);  // one shift and one multiply-add per bit
-    return ~m;
+    for (int i = 7; i >= 0; --i) {
+        m0 = __funnelshift_l(v[i], m0, 1);
+        m1 = __funnelshift_l(v[8 + i], m1, 1);
+        m2 = __funnelshift_l(v[16 + i], m2, 1);
+        m3 = __funnelshift_l(v[24 + i], m3, 1);
+    }
+    return ~(m0 | (m1 << 8) | (m2 << 16) | (m3 << 24));
 }
 
 // The jobs of one CTA: job = blockIdx.x + k * gridDim.x, tile = job / n_mtiles,
@@ -545,20 +540,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const int64_t pos = m * kBM + q * 32 + lane;
             const bool valid = pos < p.n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + s * acc_stride;
-            // This warp's 32-column chunks grp and grp+4 (N <= 256): two TMEM loads, after
-            // which the accumulator is handed back at once; the sign-bit test (an AND over
-            // the chunk: its sign bit is clear iff some column is a candidate), the rare
-            // mask building and the staging all run on the registers.
+            // This warp's 32-column chunks grp and grp+4 (N <= 256): two TMEM loads that
+            // also return each lane's maximum over the chunk, after which the accumulator
+            // is handed back at once; the candidate test on the maxima, the rare mask
+            // building and the staging all run on the registers.
             const int ca = grp, cb = grp + 4;
             const bool has_a = ca < nch, has_b = cb < nch;  // warp-uniform
             uint32_t va[32], vb[32];
+            float max_a = -1.f, max_b = -1.f;  // each chunk's maximum, from the loads themselves
             const long long tl0 = tick<kProf>();
             if (has_a) {
-                ptx::tmem_ld_32x32b_x32(taddr + ca * 32, va);
-                if (has_b) ptx::tmem_ld_32x32b_x32(taddr + cb * 32, vb);
+                ptx::tmem_ld_max_32x32b_x32(taddr + ca * 32, va, max_a);
+                if (has_b) ptx::tmem_ld_max_32x32b_x32(taddr + cb * 32, vb, max_b);
                 ptx::tmem_wait_ld();
                 ptx::reg_fence(va);
                 ptx::reg_fence(vb);
+                asm volatile("" : "+f"(max_a), "+f"(max_b));  // the same fence for the maxima
             }
             const long long tf0 = tick<kProf>();
             ptx::tc_fence_before();
@@ -572,9 +569,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             }
             if (has_a) {
                 const long long tr0 = tick<kProf>();
-                // sign bit of the AND clear <=> some column of the chunk is a candidate
-                const bool any_a = valid && (int32_t)and32(va) >= 0;
-                const bool any_b = has_b && valid && (int32_t)and32(vb) >= 0;
+                // maximum >= 0 <=> some column of the chunk is a candidate (a -0.0 passes
+                // here and is dropped by the sign mask, as before)
+                const bool any_a = valid && max_a >= 0.f;
+                const bool any_b = has_b && valid && max_b >= 0.f;
                 if (__any_sync(0xffffffffu, any_a || any_b)) {  // rare: stage this warp's candidates
                     ++n_rare;
                     if (__any_sync(0xffffffffu, any_a))
