@@ -474,12 +474,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
             };
             const long long t2 = tick<kProf>();
+            // the one-hot of base i is the first half of entry i and the second half of
+            // entry i - 1: computed once, stored twice
+            uint2 *e2 = reinterpret_cast<uint2 *>(e);
 #pragma unroll 2
-            for (int i = et; i < entries; i += kEWarps * 32) {
-                const int j = i + 1;
+            for (int i = et; i <= entries; i += kEWarps * 32) {
                 const uint2 a = onehot((cw[i >> 4] >> (2 * (i & 15))) & 3u, (zw[i >> 5] >> (i & 31)) & 1u);
-                const uint2 b = onehot((cw[j >> 4] >> (2 * (j & 15))) & 3u, (zw[j >> 5] >> (j & 31)) & 1u);
-                e[i] = make_uint4(a.x, a.y, b.x, b.y);
+                if (i < entries) e2[2 * i] = a;
+                if (i > 0) e2[2 * i - 1] = a;
             }
             // each writer makes its E entries visible to the tensor cores and orders its
             // reads of code stage cs before the refill below
