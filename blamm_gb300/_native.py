@@ -21,7 +21,7 @@ BLAMM_ERR_NOMEM = -5
 BLAMM_ERR_UNSUPPORTED = -6
 BLAMM_ERR_STATE = -7
 
-MODES = {"fp32": 0, "bf16": 1, "bf16x2": 2}
+MODES = {"fp32": 0, "bf16": 1, "bf16x2": 2, "auto": 3}
 
 HIT_DTYPE = np.dtype([("pos", "<i8"), ("col", "<i4"), ("score", "<f4")])
 
@@ -93,6 +93,7 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_fasta_parse_device.argtypes = [vp, vp, i64, vp, C.POINTER(i64), vp, vp, vp, C.POINTER(i64), vp,
                                              C.POINTER(i64), vp]
     lib.blamm_get_plan_options.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+    lib.blamm_get_terms.argtypes = [vp]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
@@ -100,7 +101,7 @@ def gpu_lib() -> C.CDLL:
                  "blamm_debug_profile_read", "blamm_scan_device_static", "blamm_set_columns",
                  "blamm_reserve", "blamm_scan_enqueue", "blamm_scan_graph_create", "blamm_scan_graph_launch",
                  "blamm_autotune", "blamm_theoretical_hist", "blamm_device_memory", "blamm_set_plan_options",
-                 "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall"):
+                 "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall", "blamm_get_terms"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -114,7 +115,7 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
 class GpuScanner:
     """A device context with a resident motif bank (one per host thread)."""
 
-    def __init__(self, device: int = 0, mode: str = "bf16x2"):
+    def __init__(self, device: int = 0, mode: str = "auto"):
         self.lib = gpu_lib()
         h = C.c_void_p()
         rc = self.lib.blamm_ctx_create(device, C.byref(h))
@@ -270,6 +271,10 @@ class GpuScanner:
         n, c = C.c_int(), C.c_float()
         self._check(self.lib.blamm_get_plan_options(self.h, C.byref(n), C.byref(c)))
         return n.value, c.value
+
+    def terms(self) -> int:
+        """BF16 terms of the tensor-core scan in the current mode (0 in FP32 mode)."""
+        return int(self.lib.blamm_get_terms(self.h))
 
     def autotune(self, d_bases: int, n: int, d_runs: int, nruns: int) -> float:
         ms = C.c_float(0.0)

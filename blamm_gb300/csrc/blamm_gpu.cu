@@ -33,7 +33,8 @@ struct blamm_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::string err;
-    int mode = BLAMM_MODE_BF16X2;
+    int mode = BLAMM_MODE_AUTO;
+    int auto_terms = 1;  // BLAMM_MODE_AUTO: BF16 terms in use (1 until the autotuner measured both)
     bool plain_timed = false, rescore_timed = false;
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
@@ -453,7 +454,7 @@ const char *blamm_last_error(const blamm_ctx *ctx) { return ctx ? ctx->err.c_str
 int blamm_set_mode(blamm_ctx *ctx, int mode)
 {
     if (!ctx) return BLAMM_ERR_ARG;
-    if (mode != BLAMM_MODE_FP32 && mode != BLAMM_MODE_BF16 && mode != BLAMM_MODE_BF16X2)
+    if (mode != BLAMM_MODE_FP32 && mode != BLAMM_MODE_BF16 && mode != BLAMM_MODE_BF16X2 && mode != BLAMM_MODE_AUTO)
         return fail(ctx, BLAMM_ERR_ARG, "unknown mode %d", mode);
     ctx->mode = mode;
     return BLAMM_OK;
@@ -544,9 +545,15 @@ int blamm_set_thresholds(blamm_ctx *ctx, const float *thr)
 }  // extern "C"
 
 // ------------------------------------------------------------------ drivers
+// BF16 terms of the tensor-core modes
+static int mode_terms(const blamm_ctx *ctx)
+{
+    return ctx->mode == BLAMM_MODE_BF16X2 ? 2 : ctx->mode == BLAMM_MODE_AUTO ? ctx->auto_terms : 1;
+}
+
 static int ensure_plan(blamm_ctx *ctx)
 {
-    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    const int terms = mode_terms(ctx);
     if (ctx->plan_valid && ctx->plan_terms == terms) return BLAMM_OK;
     return build_plan(ctx, terms);
 }
@@ -1124,7 +1131,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         return fail(ctx, BLAMM_ERR_ARG, "null buffer");
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     const bool tc = ctx->mode != BLAMM_MODE_FP32;
-    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    const int terms = mode_terms(ctx);
     if (tc && !(ctx->plan_valid && ctx->plan_terms == terms))
         return fail(ctx, BLAMM_ERR_STATE,
                     "blamm_scan_device_static: no tensor-core plan for this bank, mode and thresholds "
@@ -1285,7 +1292,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
         return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: %lld positions exceed the reservation",
                     (long long)n);
     const bool tc = ctx->mode != BLAMM_MODE_FP32;
-    const int terms = ctx->mode == BLAMM_MODE_BF16X2 ? 2 : 1;
+    const int terms = mode_terms(ctx);
     if (tc && (!(ctx->plan_valid && ctx->plan_terms == terms) || ctx->cand_cap <= 0))
         return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: call blamm_reserve after changing the bank, "
                                           "columns, thresholds or mode");
@@ -1410,6 +1417,12 @@ int blamm_set_plan_options(blamm_ctx *ctx, int max_tile_columns, float job_cost)
     return BLAMM_OK;
 }
 
+int blamm_get_terms(const blamm_ctx *ctx)
+{
+    if (!ctx) return 0;
+    return ctx->mode == BLAMM_MODE_FP32 ? 0 : mode_terms(ctx);
+}
+
 int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *job_cost)
 {
     if (!ctx || !max_tile_columns || !job_cost) return BLAMM_ERR_ARG;
@@ -1438,37 +1451,46 @@ int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t
     ctx->hits_cap = (int64_t)hc;
     const int nmax_opts[] = {128, 192, 256};
     const double cost_opts[] = {200.0, 700.0, 1500.0};
-    const int keep_nmax = ctx->plan_nmax;
+    const int keep_nmax = ctx->plan_nmax, keep_terms = ctx->auto_terms;
     const double keep_cost = ctx->plan_job_cost;
+    // BLAMM_MODE_AUTO also chooses the number of BF16 terms: one term halves the MMAs
+    // and widens the guard band (more candidates to rescore), so the whole call's
+    // kernel time (packing, scan, rescoring) decides
+    const int nterm_opts = ctx->mode == BLAMM_MODE_AUTO ? 2 : 1;
     float best = std::numeric_limits<float>::infinity();
-    int bn = keep_nmax;
+    int bn = keep_nmax, bt = keep_terms;
     double bc = keep_cost;
-    for (int nm : nmax_opts)
-        for (double jc : cost_opts) {
-            ctx->plan_nmax = nm;
-            ctx->plan_job_cost = jc;
-            ctx->plan_valid = false;
-            float t[3];
-            for (int rep = 0; rep < 3; ++rep) {
-                int64_t nh = 0;
-                rc = scan_core(ctx, d_bases, ns, d_run_start, nrs, ctx->d_hits, ctx->hits_cap, &nh);
-                if (rc && rc != BLAMM_ERR_OVERFLOW) {
-                    ctx->plan_nmax = keep_nmax;
-                    ctx->plan_job_cost = keep_cost;
-                    ctx->plan_valid = false;
-                    return rc;
+    for (int ti = 0; ti < nterm_opts; ++ti)
+        for (int nm : nmax_opts)
+            for (double jc : cost_opts) {
+                if (ctx->mode == BLAMM_MODE_AUTO) ctx->auto_terms = ti + 1;
+                ctx->plan_nmax = nm;
+                ctx->plan_job_cost = jc;
+                ctx->plan_valid = false;
+                float t[3];
+                for (int rep = 0; rep < 3; ++rep) {
+                    int64_t nh = 0;
+                    rc = scan_core(ctx, d_bases, ns, d_run_start, nrs, ctx->d_hits, ctx->hits_cap, &nh);
+                    if (rc && rc != BLAMM_ERR_OVERFLOW) {
+                        ctx->plan_nmax = keep_nmax;
+                        ctx->plan_job_cost = keep_cost;
+                        ctx->auto_terms = keep_terms;
+                        ctx->plan_valid = false;
+                        return rc;
+                    }
+                    t[rep] = ctx->stats.kernel_ms;
                 }
-                t[rep] = ctx->stats.scan_ms;
+                std::sort(t, t + 3);
+                if (t[1] < best) {
+                    best = t[1];
+                    bn = nm;
+                    bc = jc;
+                    bt = ctx->auto_terms;
+                }
             }
-            std::sort(t, t + 3);
-            if (t[1] < best) {
-                best = t[1];
-                bn = nm;
-                bc = jc;
-            }
-        }
     ctx->plan_nmax = bn;
     ctx->plan_job_cost = bc;
+    ctx->auto_terms = bt;
     ctx->plan_valid = false;
     if ((rc = ensure_plan(ctx))) return rc;
     if (best_ms) *best_ms = best;

@@ -50,7 +50,7 @@ void scanUsage()
                  "(default = 0.95)\n"
                  "  -pt\t--pthreshold\tcompute the motif score threshold from p-value [0..1] (default = 1E-4)\n"
                  "  -t\t--numthreads\tset the number of parallel threads [default = #cores]\n"
-                 "  -m\t--mode\t\tGPU arithmetic: bf16x2 (default), bf16 or fp32\n\n"
+                 "  -m\t--mode\t\tGPU arithmetic: auto (default), bf16x2, bf16 or fp32\n\n"
                  " [file_options]\n"
                  "  -H\t--histdir\tdirectory where the histogram file(s) are stored [default = .]\n"
                  "  -o\t--output\tfilename for the motif occurrences [default = occurences.txt]\n\n"
@@ -63,7 +63,7 @@ struct Options {
     float absThreshold = 0.0f, relThreshold = 0.95f, pvalue = 0.0001f;
     size_t numThreads = std::max(1u, std::thread::hardware_concurrency());
     std::string histdir, output = "occurrences.txt";
-    int mode = BLAMM_MODE_BF16X2;
+    int mode = BLAMM_MODE_AUTO;
 };
 
 // One GPU context per device (the reference runs one host thread per device,
@@ -251,7 +251,8 @@ int runScanModule(int argc, char **argv)
             if (m == "fp32") o.mode = BLAMM_MODE_FP32;
             else if (m == "bf16") o.mode = BLAMM_MODE_BF16;
             else if (m == "bf16x2") o.mode = BLAMM_MODE_BF16X2;
-            else throw std::runtime_error("unknown mode " + m + " (bf16x2, bf16 or fp32)");
+            else if (m == "auto") o.mode = BLAMM_MODE_AUTO;
+            else throw std::runtime_error("unknown mode " + m + " (auto, bf16x2, bf16 or fp32)");
         } else {
             scanUsage();
             exit(EXIT_FAILURE);

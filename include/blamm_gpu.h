@@ -46,6 +46,8 @@ extern "C" {
 #define BLAMM_MODE_FP32 0   /* plain SIMT FP32 sums: the straightforward GPU form */
 #define BLAMM_MODE_BF16 1   /* tcgen05, P as one BF16 term, wide guard band */
 #define BLAMM_MODE_BF16X2 2 /* tcgen05, P split hi+lo BF16 (two MMAs), narrow guard band */
+#define BLAMM_MODE_AUTO 3   /* tcgen05 with one or two BF16 terms, whichever blamm_autotune
+                               measured faster on its sample (one term until then) */
 
 typedef struct blamm_ctx blamm_ctx;
 
@@ -81,7 +83,8 @@ int blamm_ctx_create(int device, blamm_ctx **out);
 void blamm_ctx_destroy(blamm_ctx *ctx);
 const char *blamm_last_error(const blamm_ctx *ctx);
 
-/* Select the arithmetic (BLAMM_MODE_*).  Default BLAMM_MODE_BF16X2. */
+/* Select the arithmetic (BLAMM_MODE_*).  Default BLAMM_MODE_AUTO.  Every mode
+ * emits the same hits and bit-identical scores; they differ in speed only. */
 int blamm_set_mode(blamm_ctx *ctx, int mode);
 
 /* Upload the motif bank.  P is MotifContainer's matrix (src/motif.cpp:542-564):
@@ -160,9 +163,11 @@ void blamm_scan_graph_destroy(void *graph);
 
 /* Autotuner: time the tensor-core scan of the first min(n, 16 Mi) positions
  * (device data) under several tile plans -- widest N tile 128 / 192 / 256 x
- * the planner's fixed cost per job -- and keep the fastest plan for later
- * scans of this context.  *best_ms (optional) receives its kernel time.
- * Nothing to tune in BLAMM_MODE_FP32. */
+ * the planner's fixed cost per job, and in BLAMM_MODE_AUTO one and two BF16
+ * terms -- and keep the fastest for later scans of this context (the time of
+ * all kernels of the call: packing, scan, rescoring; median of three).
+ * *best_ms (optional) receives that time.  Nothing to tune in BLAMM_MODE_FP32.
+ * The chosen term count: blamm_get_terms. */
 int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
                    int64_t nruns, float *best_ms);
 
@@ -170,6 +175,8 @@ int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t
  * columns; at most 128 gives four TMEM accumulators instead of two) and the
  * fixed cycles per job of its cost model.  Setting them replans. */
 int blamm_set_plan_options(blamm_ctx *ctx, int max_tile_columns, float job_cost);
+/* BF16 terms the tensor-core scan uses in the current mode (1 or 2; 0 for FP32). */
+int blamm_get_terms(const blamm_ctx *ctx);
 int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *job_cost);
 
 /* The hist module's theoretical histograms and p-value thresholds on the GPU

@@ -25,6 +25,6 @@ def _built():
 @pytest.fixture(scope="session")
 def scanner():
     from blamm_gb300 import GpuScanner
-    s = GpuScanner(0)
+    s = GpuScanner(0, "bf16x2")
     yield s
     s.close()

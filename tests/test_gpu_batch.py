@@ -127,6 +127,33 @@ def test_autotune_keeps_the_hit_set(scanner):
     assert ok, msg
 
 
+def test_auto_mode_chooses_a_term_count_and_keeps_the_hit_set():
+    """The default mode: one BF16 term until the autotuner has timed one and two terms
+    on its sample; either way the hits equal the oracle's."""
+    torch = _torch()
+    from blamm_gb300 import GpuScanner
+    P, lens, thr = make_bank(53, 160, 5, 30, rel=0.85)
+    bases, runs = make_stream(54, 1_500_000, nruns=4)
+    sc = GpuScanner(0)
+    try:
+        assert sc.mode == "auto"
+        sc.set_motifs(P, lens, thr)
+        assert sc.terms() == 1
+        want = oracle.scan(bases, runs, P, lens, thr)
+        ok, msg = same_hits(sc.scan(bases, runs), want)
+        assert ok, msg
+        d_b = torch.from_numpy(bases).cuda()
+        d_r = torch.from_numpy(runs).cuda()
+        assert sc.autotune(d_b.data_ptr(), len(bases), d_r.data_ptr(), len(runs)) > 0
+        assert sc.terms() in (1, 2)
+        ok, msg = same_hits(sc.scan(bases, runs), want)
+        assert ok, msg
+        sc.set_mode("fp32")
+        assert sc.terms() == 0
+    finally:
+        sc.close()
+
+
 def test_many_short_sequences_one_call_equals_one_call_each(scanner):
     """Batching: 600 promoter-like sequences in one stream (one run each) give, per
     sequence, exactly the hits of that sequence scanned alone."""
