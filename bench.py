@@ -47,6 +47,9 @@ def args_parse():
     ap.add_argument("--cpu-sample", type=int, default=8_000_000, help="bases in a CPU-baseline sample")
     ap.add_argument("--no-modes", action="store_true", help="skip the bf16 / fp32 comparison runs")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--mode", default="auto", choices=["auto", "bf16", "bf16x2"],
+                    help="headline arithmetic: auto (the library default, autotuned on a sample) or a fixed "
+                         "term count with the default tile plan (no autotuner launches, for profiling)")
     ap.add_argument("--serve-requests", type=int, default=48, help="distinct requests of the serving pool")
     ap.add_argument("--serve-slots", type=int, default=8, help="requests in flight in the serving measurement")
     ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4"],
@@ -148,14 +151,16 @@ def peaks():
     return 1900.0, "fallback 1.9 PFLOP/s"
 
 
-def profile_traffic(positions: int):
-    """DRAM bytes of one scan-kernel launch, scaled from the committed ncu summary."""
+def profile_traffic(positions: int, terms: int):
+    """DRAM bytes of one scan-kernel launch (the instance for `terms` BF16 terms), scaled by
+    positions from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "scan_tc_traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    return int(d["dram_bytes"] * positions / d["positions"])
+    b = d["dram_bytes_by_terms"].get(str(terms))
+    return None if b is None else int(b * positions / d["positions"])
 
 
 def hit_digest(h: np.ndarray) -> tuple[int, int]:
@@ -413,13 +418,14 @@ def run_config3(a):
 def run_config4(a):
     """Config 4: 10,000 promoter-like sequences (log-normal lengths, median 2 kbp, sigma 1.0,
     clipped 200 bp-50 kbp, GC 0.5) x 800 motifs (1600 columns), p = 1e-4: one persistent launch
-    over all sequences, the same as a CUDA graph, and one launch per sequence; autotuned plan."""
+    over all sequences, the same as a CUDA graph, and one launch per sequence, in the default mode
+    (one BF16 term until tuned); then the autotuned term count and plan."""
     import torch
     from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
     wl = workloads.config4(a.seed)
     bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
     counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
-    sc = GpuScanner(0, "bf16x2")
+    sc = GpuScanner(0, "auto")
     P, lens, thr, _ = _bank_for(wl.motifs, counts, (1e-4,), sc)
     sc.set_motifs(P, lens, thr[0])
     n, ncols = len(bases), P.shape[0]
@@ -474,7 +480,8 @@ def run_config4(a):
            "graph_ms": graph_ms, "graph_bp_motif_per_s": units / (graph_ms / 1e3),
            "per_sequence_launches_ms": per_seq_ms, "per_sequence_bp_motif_per_s": units / (per_seq_ms / 1e3),
            "per_sequence_sample": f"first {k} sequences, extrapolated to all",
-           "autotuned_ms": tuned, "autotune_plan": list(sc.plan_options()), "autotuned_same_hits": same,
+           "autotuned_ms": tuned, "autotune_plan": list(sc.plan_options()), "autotune_terms": sc.terms(),
+           "autotuned_same_hits": same,
            "hits": int(nh)}
     sc.close()
     print(json.dumps({"metric": METRIC, "config": out}), flush=True)
@@ -497,14 +504,14 @@ def run_ours(a, rank, world, local):
     units = n * ncols
     flops_per_bp = float(8 * lens.astype(np.int64).sum())
 
-    sc = GpuScanner(local, "auto")
+    sc = GpuScanner(local, a.mode)
     sc.set_motifs(P, lens, thr)
     ext = torch.cuda.ExternalStream(sc.stream())
     d_bases = torch.from_numpy(bases).to(f"cuda:{local}")
     d_runs = torch.from_numpy(runs).to(f"cuda:{local}")
     # the library's default mode picks one or two BF16 terms (and the tile plan) from timed
     # scans of a 16 Mi-position sample of the stream; untimed, as a deployment would do once
-    tuned_ms = sc.autotune(d_bases.data_ptr(), n, d_runs.data_ptr(), len(runs))
+    tuned_ms = sc.autotune(d_bases.data_ptr(), n, d_runs.data_ptr(), len(runs)) if a.mode == "auto" else None
     terms = sc.terms()
     tuned = {"terms": terms, "max_tile_columns": sc.plan_options()[0], "job_cost": sc.plan_options()[1],
              "sample_kernel_ms": tuned_ms}
@@ -586,6 +593,10 @@ def run_ours(a, rank, world, local):
     # ---- other modes on the same stream (same hits required)
     modes = {}
     if not a.no_modes:
+        # each fixed form with the library's default tile plan (the autotuned knobs suit the
+        # headline's term count)
+        keep_plan = sc.plan_options()
+        sc.set_plan_options(256, 700.0)
         for mode in ("bf16x2", "bf16", "fp32"):
             sc.set_mode(mode)
             device_steps(1, False)
@@ -595,7 +606,8 @@ def run_ours(a, rank, world, local):
                            "scan_kernel_ms": float(np.mean(msc)), "hits": int(mnh),
                            "candidates": int(mst["candidates"]),
                            "same_hits_as_headline": hit_digest(hits_on_device(mnh)) == ref_digest}
-        sc.set_mode("auto")
+        sc.set_mode(a.mode)
+        sc.set_plan_options(*keep_plan)
 
     # ---- score error of the tensor-core sums against FP64 (emitted scores are rescored in FP32)
     precision = {}
@@ -605,21 +617,22 @@ def run_ours(a, rank, world, local):
         for mode in ("bf16x2", "bf16"):
             sc.set_mode(mode)
             precision["mma_" + mode] = mma_score_error(sc, bases, P, lens, ref, npos)
-        sc.set_mode("auto")
+        sc.set_mode(a.mode)
         precision["emitted"] = emitted_score_error(hits_on_device(nh), ref, npos)
 
     # ---- roofline of the dominant kernel (tcgen05 scan)
     peak, peak_src = peaks()
     kern_ms = float(np.mean(scan_ms))
     achieved = n * flops_per_bp / (kern_ms / 1e3) / 1e12
-    traffic = profile_traffic(n)
+    traffic = profile_traffic(n, terms)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": ("bf16x2 (hi+lo fixed-point split" if terms == 2 else "bf16 (one fixed-point term")
-                 + ", fp32 accumulate) + fp32 rescoring; term count autotuned",
+                 + ", fp32 accumulate) + fp32 rescoring"
+                 + ("; term count autotuned" if a.mode == "auto" else ""),
         "data": "synthetic (seeded numpy, config2 shapes)",
         "config": {"workload": "config2: 512 motifs (1024 columns, L 5-30, both strands, Dirichlet(0.5) "
                                "columns of 100 counts) x 24 iid sequences (A=T=0.29) log-uniform 1-20 Mbp, "
