@@ -82,6 +82,8 @@ struct blamm_ctx {
     size_t cap_bases = 0;
     uint32_t *d_seq2 = nullptr, *d_zmask = nullptr;
     size_t cap_words32 = 0, cap_zmask = 0;
+    uint4 *d_e16 = nullptr;  // one-hot entries of the packed stream (tensor-core A operand windows)
+    size_t cap_e16 = 0;
     int64_t *d_runs = nullptr;
     size_t cap_runs = 0;
     unsigned long long *d_cand = nullptr;
@@ -196,9 +198,8 @@ static int build_plan(blamm_ctx *ctx, int terms)
     const int gmax_all = std::max(1, (lmax_sel + 3) / 4);
     const int erows_all = kBM + 4 * gmax_all + 8;
     const long long smem_limit = (long long)ctx->max_smem;
-    // everything but the B tiles (E stages, bias A tile, code ring, candidate staging, ...)
+    // everything but the B tiles (E stages, bias A tile, candidate staging, ...)
     const long long other = (long long)kEStages * erows_all * 16 + 4096 +
-                            (long long)kCodeStages * (code_seq_bytes(erows_all) + code_zm_bytes(erows_all)) +
                             (long long)kEpiWarps * kCandBuf * 8 + 256LL * sizeof(TileDesc) + 64 + 128 + 64 + 2048 +
                             1024;
     const long long b_term_cap = (smem_limit - other) / terms;
@@ -438,7 +439,7 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     void *bufs[] = {ctx->d_P,      ctx->d_len,   ctx->d_thr,      ctx->d_tiles, ctx->d_bbuf,
-                    ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask,
+                    ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask, ctx->d_e16,
                     ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status,
                     ctx->d_active};
     for (void *b : bufs)
@@ -558,6 +559,16 @@ static int ensure_plan(blamm_ctx *ctx)
     return build_plan(ctx, terms);
 }
 
+// One-hot entries of a packed stream of n positions: the scan's E windows read up to
+// entry n + 127 + 4 * 64 + 2, and e16_kernel reads base i + 1 of the padded stream.
+static int64_t e16_entries(int64_t n) { return n + kStreamPad - 64; }
+
+static void launch_e16(const uint32_t *seq2, const uint32_t *zmask, int64_t n, uint4 *e16, cudaStream_t st)
+{
+    const int64_t ne = e16_entries(n);
+    e16_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(seq2, zmask, ne, e16);
+}
+
 static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
 {
     const int64_t nwords32 = (n + kStreamPad + 31) / 32;
@@ -570,16 +581,20 @@ static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
     pack_kernel<<<(unsigned)blocks, threads, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
                                                                nwords32, ctx->lower_scores);
     CK(cudaGetLastError());
+    if (ctx->mode != BLAMM_MODE_FP32) {
+        rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(n));
+        if (rc) return rc;
+        launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
+    }
     return BLAMM_OK;
 }
 
 // Kernel parameters of the current plan over a packed stream of n positions
 // (the caller adds candidates, counters, status and the test hooks).
-static TcParams tc_params(const blamm_ctx *ctx, const uint32_t *seq2, const uint32_t *zmask, int64_t n)
+static TcParams tc_params(const blamm_ctx *ctx, const uint4 *e16, int64_t n)
 {
     TcParams p{};
-    p.seq2 = seq2;
-    p.zmask = zmask;
+    p.e16 = e16;
     p.n = n;
     p.n_mtiles = (n + kBM - 1) / kBM;
     p.tiles = ctx->d_tiles;
@@ -636,7 +651,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     for (int attempt = 0; attempt < 3; ++attempt) {
         CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-        TcParams p = tc_params(ctx, ctx->d_seq2, ctx->d_zmask, n);
+        TcParams p = tc_params(ctx, ctx->d_e16, n);
         p.cand = ctx->d_cand;
         p.cand_count = ctx->d_counters;
         p.cand_cap = ctx->cand_cap;
@@ -767,7 +782,7 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     int rc = launch_pack(ctx, d_bases, n);
     if (rc) return rc;
-    ++launches;
+    launches += ctx->mode == BLAMM_MODE_FP32 ? 1 : 2;  // packing (+ one-hot entries)
     if (ctx->mode == BLAMM_MODE_FP32) rc = run_plain(ctx, n, d_runs, nruns, d_hits, hit_cap, &launches);
     else rc = run_tc(ctx, n, d_runs, nruns, d_hits, hit_cap, nullptr, 0, 0, &launches);
     if (rc) return rc;
@@ -1078,16 +1093,17 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
 
 namespace {
 
-constexpr int64_t kStaticMaxBases = int64_t(8) << 20;  // positions per call
+constexpr int64_t kStaticMaxBases = int64_t(4) << 20;  // positions per call
 constexpr int64_t kStaticWords32 = (kStaticMaxBases + kStreamPad + 31) / 32;
-constexpr int64_t kStaticCandCap = int64_t(2) << 20;   // tensor-core candidates per call
+constexpr int64_t kStaticCandCap = int64_t(1) << 20;   // tensor-core candidates per call
 constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kStaticSeq2Off = 0;
 constexpr size_t kStaticZmaskOff = round256(kStaticSeq2Off + sizeof(uint32_t) * 2 * kStaticWords32);
-constexpr size_t kStaticCandOff = round256(kStaticZmaskOff + sizeof(uint32_t) * kStaticWords32);
+constexpr size_t kStaticE16Off = round256(kStaticZmaskOff + sizeof(uint32_t) * kStaticWords32);
+constexpr size_t kStaticCandOff = round256(kStaticE16Off + sizeof(uint4) * (kStaticMaxBases + kStreamPad));
 constexpr size_t kStaticCountOff = round256(kStaticCandOff + sizeof(unsigned long long) * kStaticCandCap);
 constexpr size_t kStaticStatusOff = round256(kStaticCountOff + sizeof(unsigned long long) * 4);
-constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 19 MiB
+constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 73 MiB
 
 constexpr int kStaticMaxDevices = 64;
 
@@ -1142,6 +1158,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
     if (rc) return rc;
     uint32_t *seq2 = reinterpret_cast<uint32_t *>(base + kStaticSeq2Off);
     uint32_t *zmask = reinterpret_cast<uint32_t *>(base + kStaticZmaskOff);
+    uint4 *e16 = reinterpret_cast<uint4 *>(base + kStaticE16Off);
     unsigned long long *cand = reinterpret_cast<unsigned long long *>(base + kStaticCandOff);
     unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + kStaticCountOff);
     int *status = reinterpret_cast<int *>(base + kStaticStatusOff);
@@ -1158,6 +1175,11 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
                                                                           ctx->lower_scores);
     CK(cudaGetLastError());
     ++launches;
+    if (tc) {
+        launch_e16(seq2, zmask, n, e16, ctx->stream);
+        CK(cudaGetLastError());
+        ++launches;
+    }
 
     if (!tc) {
         PlainParams p{};
@@ -1194,7 +1216,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         if ((int)L.total > ctx->max_smem)
             return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
         const uint32_t smem = std::max<uint32_t>(L.total, 116 * 1024);
-        TcParams p = tc_params(ctx, seq2, zmask, n);
+        TcParams p = tc_params(ctx, e16, n);
         p.cand = cand;
         p.cand_count = counters;
         p.cand_cap = kStaticCandCap;
@@ -1271,6 +1293,7 @@ int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
     if (rc) return rc;
     if (ctx->mode != BLAMM_MODE_FP32) {
         if ((rc = ensure_plan(ctx))) return rc;
+        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(max_positions)))) return rc;
         if (max_candidates > ctx->cand_cap) {
             size_t cap = ctx->cand_cap > 0 ? (size_t)ctx->cand_cap : 0;
             rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)max_candidates);
@@ -1293,7 +1316,8 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
                     (long long)n);
     const bool tc = ctx->mode != BLAMM_MODE_FP32;
     const int terms = mode_terms(ctx);
-    if (tc && (!(ctx->plan_valid && ctx->plan_terms == terms) || ctx->cand_cap <= 0))
+    if (tc && (!(ctx->plan_valid && ctx->plan_terms == terms) || ctx->cand_cap <= 0 ||
+               (size_t)e16_entries(n) > ctx->cap_e16))
         return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: call blamm_reserve after changing the bank, "
                                           "columns, thresholds or mode");
     if (n > 0 && (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits)))
@@ -1305,6 +1329,10 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     pack_kernel<<<(unsigned)((nwords32 + 255) / 256), 256, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
                                                                           nwords32, ctx->lower_scores);
     CK(cudaGetLastError());
+    if (tc) {
+        launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
+        CK(cudaGetLastError());
+    }
     if (!tc) {
         PlainParams p{};
         p.seq2 = ctx->d_seq2;
@@ -1339,7 +1367,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
-    TcParams p = tc_params(ctx, ctx->d_seq2, ctx->d_zmask, n);
+    TcParams p = tc_params(ctx, ctx->d_e16, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
     p.cand_cap = ctx->cand_cap;

@@ -76,6 +76,25 @@ __global__ void pack_kernel(const char *__restrict__ bases, int64_t n, uint32_t 
     zmask[w] = z;
 }
 
+// One-hot entries for the tensor-core scan: E[i] = onehot(base i) ++ onehot(base i+1),
+// 4 bf16 channels per base (1.0 = 0x3F80 in channel code, zeros for a zero-masked base).
+__device__ __forceinline__ uint2 onehot_bf16(uint32_t code, uint32_t zero)
+{
+    const uint32_t h = zero ? 0u : (0x3F80u << ((code & 1u) << 4));
+    return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
+}
+
+__global__ void e16_kernel(const uint32_t *__restrict__ seq2, const uint32_t *__restrict__ zmask, int64_t ne,
+                           uint4 *__restrict__ e16)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ne) return;
+    const int64_t j = i + 1;
+    const uint2 a = onehot_bf16((seq2[i >> 4] >> (2 * (i & 15))) & 3u, (zmask[i >> 5] >> (i & 31)) & 1u);
+    const uint2 b = onehot_bf16((seq2[j >> 4] >> (2 * (j & 15))) & 3u, (zmask[j >> 5] >> (j & 31)) & 1u);
+    e16[i] = make_uint4(a.x, a.y, b.x, b.y);
+}
+
 // ------------------------------------------------------------------------
 // 2. plain FP32 scan: one thread per position, sequential FP32 sums
 //    (the straightforward GPU form of PWMScan::scanThreadBLAS + extractOccurrences)

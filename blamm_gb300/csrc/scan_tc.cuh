@@ -2,11 +2,12 @@
 // one persistent CTA per SM.
 //
 // Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
-// For an M tile of 128 positions starting at m0, the E-builder warps write
-// one 16-byte entry per position, E[i] = onehot(base m0+i) ++ onehot(base
-// m0+i+1) (2 bases x 4 channels x bf16).  Read with row stride 16 B, 8-row
-// group stride (SBO) 128 B and K-core stride (LBO) 32 B, the entries starting
-// at E[4g] form exactly the A operand of motif bases 4g..4g+3 for all 128
+// The packing kernel writes one 16-byte entry per stream position,
+// E[i] = onehot(base i) ++ onehot(base i+1) (2 bases x 4 channels x bf16).
+// For an M tile of 128 positions starting at m0, a bulk copy brings entries
+// m0 .. m0+128+4g+1 into shared memory; read with row stride 16 B, 8-row group
+// stride (SBO) 128 B and K-core stride (LBO) 32 B, the entries starting at
+// E[4g] form exactly the A operand of motif bases 4g..4g+3 for all 128
 // positions -- the overlapping one-hot windows of the reference's S matrix
 // (src/sequence.cpp:299-340) without materialising them: each k-step is a
 // shifted A descriptor over the same ~150 entries.  B_g holds rows
@@ -26,23 +27,23 @@
 // in exact FP32 (rescore_kernel).
 //
 // Roles (640 threads): warps 0-15 drain TMEM (lane quarter = warp % 4, column
-// group = warp / 4) and test for candidates; warp 16 allocates TMEM and one lane
-// issues the MMAs and the TMA bulk copies of B tiles; warps 17-19 build E from
-// 2-bit code windows that one of their threads prefetches with TMA bulk copies
-// kCodeStages jobs ahead.  kEStages E stages and 2 or 4 TMEM accumulator stages (4 when
-// the plan's N tiles are at most 128 wide) keep the roles overlapped.  A drain warp
-// hands its accumulator back right after its TMEM loads; the sign test and the
-// staging of candidates run on registers while the MMAs of the next job proceed.
-// Start-signal hand-off (two-term instances): the issuing thread waits on one
-// barrier per job and commits once.  The accumulator stage's empty barrier
-// then counts the drain warps and the E builders' first thread, so that its
-// phase completes when the stage is drained AND the job's E stage is built;
-// a drain thread signals E empty once the job's MMAs are complete.
-// Jobs (N tile, M tile) are statically interleaved over the CTAs, N-tile
-// major, so a CTA reloads B only when its tile changes.  Every wait is an
-// mbarrier try-wait that sleeps and is bounded: on a timeout the CTA raises an
-// abort flag, every role stops, copies and MMAs in flight are drained, TMEM is
-// freed and the status word tells the host.
+// group = warp / 4) and test for candidates; warps 16 and 17 (one lane each)
+// issue the MMAs of the even and the odd jobs, so that one issuer's waits,
+// commits and loop overhead overlap the other's MMAs (a thread issues about
+// one 128x256x16 MMA per 128 cycles, and a job's result reaches the drain
+// warps some 600 cycles after its last MMA); warp 18 (one lane) loads B tiles
+// and E windows with TMA bulk copies up to kEStages jobs ahead; warp 16 also
+// allocates TMEM.  kEStages E stages and 2 or 4 TMEM accumulator stages (4
+// when the plan's N tiles are at most 128 wide) keep the roles overlapped.  A
+// drain warp hands its accumulator back right after its TMEM loads; the
+// candidate test and the staging of candidates run on registers while the
+// MMAs of the next jobs proceed.  Jobs (N tile, M tile) are statically
+// interleaved over the CTAs, N-tile major, so a CTA reloads B only when its
+// tile changes: both issuers commit their old-tile MMAs to a tile-done
+// barrier, the loader then copies the new B, and both wait for it.  Every wait
+// is an mbarrier try-wait that sleeps and is bounded: on a timeout the CTA
+// raises an abort flag, every role stops, copies and MMAs in flight are
+// drained, TMEM is freed and the status word tells the host.
 #pragma once
 #include <cstdint>
 
@@ -56,13 +57,11 @@ constexpr int kBM = 128;         // positions per M tile (= UMMA M)
 constexpr int kMaxTcLen = BLAMM_MAX_TC_MOTIF_LEN;  // longest motif on the tensor-core path
 constexpr int kCandBuf = 128;    // per-warp staging of candidates in SMEM
 constexpr int kEpiWarps = 16;    // TMEM drain warps (4 per lane quarter)
-constexpr int kMmaWarp = 16;
-constexpr int kWWarp = 17;      // first of the E-builder warps
-constexpr int kEWarps = 3;       // E-builder warps 17-19
-constexpr int kEBarrier = 1;     // named barrier of the E builders
+constexpr int kMmaWarp = 16;     // issuer of the even jobs; TMEM allocation
+constexpr int kMmaWarp2 = 17;    // issuer of the odd jobs
+constexpr int kLoadWarp = 18;    // TMA bulk copies of B tiles and E windows
 constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps)
-constexpr int kCodeStages = 4;   // code windows in flight
-constexpr int kEStages = 6;      // one-hot E stages
+constexpr int kEStages = 6;      // E windows in flight
 constexpr int kMaxAcc = 4;       // TMEM accumulator stages (at most)
 
 // Per-N-tile description (host-built, staged in SMEM by the kernel).
@@ -76,8 +75,7 @@ struct TileDesc {
 };
 
 struct TcParams {
-    const uint32_t *seq2;
-    const uint32_t *zmask;
+    const uint4 *e16;    // one-hot entries of the stream (16 B per position, padded)
     int64_t n;           // stream positions
     int64_t n_mtiles;    // ceil(n / 128)
     const TileDesc *tiles;
@@ -103,20 +101,17 @@ struct TcParams {
     long long *prof;
 };
 
-// tc_prof_fields: 0 MMA wait acc_empty, 1 MMA wait E full, 2 MMA B reloads, 3 MMA loop,
-// 4 E wait code window, 5 E wait E empty, 6 epilogue hand-back (fence + arrive),
-// 7 epilogue wait acc_full, 8 epilogue loop, 9 epilogue drain (acc_full -> acc_empty
-// arrive), 10 jobs, 11 E-builder build time, 12 epilogue rounds with a candidate,
-// 13 epilogue TMEM loads, 14 epilogue fence after the wait, 15 epilogue sign test and
-// staging, 16-23 drain time of epilogue warps 0-7, 24-31 their accumulator waits
-
-// bytes of one prefetched code window (2-bit codes and zero mask) for erows entries
-__host__ __device__ inline uint32_t code_seq_bytes(int erows) { return (uint32_t)(((erows + 2 + 15) / 16 * 4 + 15) / 16 * 16); }
-__host__ __device__ inline uint32_t code_zm_bytes(int erows) { return (uint32_t)(((erows + 2 + 31) / 32 * 4 + 15) / 16 * 16); }
+// tc_prof_fields: 0/1 issuers' waits for a drained accumulator, 2 issuers' waits for B
+// tiles, 3 MMA loop, 4 loader waits for free E stages, 5 loader waits at tile changes,
+// 6 epilogue hand-back (fence + arrive), 7 epilogue wait acc_full, 8 epilogue loop,
+// 9 epilogue drain (acc_full -> acc_empty arrive), 10 jobs, 11 issuers' waits for E,
+// 12 epilogue rounds with a candidate, 13 epilogue TMEM loads, 14 epilogue fence after
+// the wait, 15 epilogue sign test and staging, 16-23 drain time of epilogue warps 0-7,
+// 24-31 their accumulator waits
 
 struct TcSmem {
     // byte offsets into dynamic shared memory
-    uint32_t b_hi, b_lo, e0, abias, codes, cand, tiles, bars, misc, total;
+    uint32_t b_hi, b_lo, e0, abias, cand, tiles, bars, misc, total;
 };
 
 __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms, int erows, int ntiles)
@@ -133,7 +128,6 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms,
     L.b_lo = take(terms == 2 ? b_term_max : 0, 1024);
     L.e0 = take((uint32_t)kEStages * erows * 16, 128);  // kEStages stages of erows entries
     L.abias = take(16 * 256, 128);  // 128 rows x 16 K-elements, canonical K-major layout
-    L.codes = take(kCodeStages * (code_seq_bytes(erows) + code_zm_bytes(erows)), 128);
     L.cand = take(kEpiWarps * kCandBuf * 8, 16);
     L.tiles = take((uint32_t)ntiles * sizeof(TileDesc), 16);
     L.bars = take(32 * 8, 8);  // BAR_COUNT <= 32
@@ -143,14 +137,14 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms,
 }
 
 enum {
-    BAR_WFULL = 0,                       // E stage built        (kEStages)
-    BAR_WEMPTY = BAR_WFULL + kEStages,   // E stage consumed     (kEStages)
-    BAR_AFULL = BAR_WEMPTY + kEStages,   // accumulator ready    (kMaxAcc)
-    BAR_AEMPTY = BAR_AFULL + kMaxAcc,    // accumulator drained  (kMaxAcc)
+    BAR_WFULL = 0,                       // E window landed       (kEStages)
+    BAR_WEMPTY = BAR_WFULL + kEStages,   // E window consumed     (kEStages)
+    BAR_AFULL = BAR_WEMPTY + kEStages,   // accumulator ready     (kMaxAcc)
+    BAR_AEMPTY = BAR_AFULL + kMaxAcc,    // accumulator drained   (kMaxAcc)
     BAR_BFULL = BAR_AEMPTY + kMaxAcc,    // B tile landed
-    BAR_DRAIN = BAR_BFULL + 1,           // MMAs drained
-    BAR_CODE = BAR_DRAIN + 1,            // code window landed   (kCodeStages)
-    BAR_NEVER = BAR_CODE + kCodeStages,  // never completed (the stall test hook)
+    BAR_TILE = BAR_BFULL + 1,            // both issuers done with the old B tile
+    BAR_DRAIN = BAR_TILE + 1,            // an issuer's MMAs drained (2)
+    BAR_NEVER = BAR_DRAIN + 2,           // never completed (the stall test hook)
     BAR_COUNT = BAR_NEVER + 1
 };
 static_assert(BAR_COUNT <= 32, "the barrier area holds 32 mbarriers");
@@ -267,18 +261,14 @@ __device__ __forceinline__ long long tick()
 
 // kDump: also write the raw accumulator of some positions (test hook);
 // kProf: role timing into p.prof; kTerms: p.terms (1 or 2).  The scan itself
-// is <false, false, p.terms>.  The issuing thread runs once per MMA and per
-// job, so every branch taken out of its loop at compile time shows in the scan
-// time (runtime mode switches cost 2-4 %).
+// is <false, false, p.terms>.  The issuing threads run once per MMA and per
+// job, so every branch taken out of their loops at compile time shows in the
+// scan time (runtime mode switches cost 2-4 %).
 template <bool kDump, bool kProf, int kTerms>
 __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = smem_raw + ((1024 - (ptx::smem_addr(smem_raw) & 1023)) & 1023);
-    // two terms: a job's MMAs take long enough that one start signal per job pays (7.5 %
-    // on a 40 Mbp stream x 1024 columns); with one term the E builders, which then may
-    // run only as far ahead as the accumulator stages, fall behind (6 % slower)
-    constexpr bool kStartSignal = kTerms == 2;
     const TcSmem L = tc_smem_layout(p.b_term_max, kTerms, p.erows, p.ntiles);
     const uint32_t sbase = ptx::smem_addr(smem);
     unsigned long long *s_cand = reinterpret_cast<unsigned long long *>(smem + L.cand);
@@ -286,7 +276,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     const uint32_t bars = sbase + L.bars;
     volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L.misc);
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(smem + L.misc + 4);
-    const uint32_t seq_bytes = code_seq_bytes(p.erows), zm_bytes = code_zm_bytes(p.erows);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -309,15 +298,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         }
         for (int s = 0; s < kMaxAcc; ++s) {
             ptx::mbar_init(bars + 8 * (BAR_AFULL + s), 1);
-            // start-signal hand-off: the E builders arrive too; the drain warps' share of
-            // the first phase (no earlier job to drain) is pre-arrived
-            ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps + (kStartSignal ? 1 : 0));
-            if (kStartSignal)
-                for (int k = 0; k < kEpiWarps; ++k) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
+            ptx::mbar_init(bars + 8 * (BAR_AEMPTY + s), kEpiWarps);
         }
         ptx::mbar_init(bars + 8 * BAR_BFULL, 1);
-        ptx::mbar_init(bars + 8 * BAR_DRAIN, 1);
-        for (int s = 0; s < kCodeStages; ++s) ptx::mbar_init(bars + 8 * (BAR_CODE + s), 1);
+        ptx::mbar_init(bars + 8 * BAR_TILE, 2);
+        ptx::mbar_init(bars + 8 * (BAR_DRAIN + 0), 1);
+        ptx::mbar_init(bars + 8 * (BAR_DRAIN + 1), 1);
         ptx::mbar_init(bars + 8 * BAR_NEVER, 1);
         ptx::fence_mbar_init();
     }
@@ -334,57 +320,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     const uint32_t acc_shift = p.acc_stages == 4 ? 2u : 1u, acc_mask = (uint32_t)p.acc_stages - 1u;
     const long long njobs = (long long)p.ntiles * p.n_mtiles;
 
-    if (warp == kMmaWarp) {
-        // =========================== MMA issuer ===========================
-        if (lane == 0) {
-            int cur_tile = -1;
-            uint32_t bphase = 0, dphase = 0, idesc = 0, g_steps = 0;
-            uint64_t bdesc_hi0 = 0, bdesc_lo0 = 0;  // k-step 0 of the current tile's B terms
-            long long t_acc = 0, t_w = 0, t_b = 0;
-            const long long t_start = tick<kProf>();
-            const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
-            uint32_t jc = 0;
-            bool ok = true, b_pending = false;
-            if (p.debug_stall) ok = ptx::mbar_wait(bars + 8 * BAR_NEVER, 0, s_abort, p.wait_limit);
-            JobIter it;
-            for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
-                const int tile = it.tile;
-                if (tile != cur_tile) {
-                    const long long tb = tick<kProf>();
-                    if (cur_tile >= 0) {  // every MMA reading the old B must be done
-                        ptx::mma_commit(bars + 8 * BAR_DRAIN);
-                        ok = ptx::mbar_wait(bars + 8 * BAR_DRAIN, dphase, s_abort, p.wait_limit);
-                        dphase ^= 1;
-                        if (!ok) break;
-                    }
-                    const TileDesc td = s_tiles[tile];
-                    ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * kTerms);
-                    ptx::bulk_g2s(sbase + L.b_hi, p.bbuf + td.b_off, (uint32_t)td.b_bytes,
-                                  bars + 8 * BAR_BFULL);
-                    if (kTerms == 2)
-                        ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes,
-                                      (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
-                    b_pending = true;
-                    ok = ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit);
-                    if (!ok) break;
-                    b_pending = false;
-                    bphase ^= 1;
-                    cur_tile = tile;
-                    if (kProf) t_b += tick<kProf>() - tb;
-                    g_steps = (uint32_t)td.g;
-                    idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
-                    const uint32_t sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
-                    bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
-                    bdesc_lo0 = ptx::smem_desc(sbase + L.b_lo, 128u, sbo_b);
-                }
-                const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;     // accumulator
-                const uint32_t es = jc % kEStages, eph = (jc / kEStages) & 1u;   // E stage
+    if ((warp == kMmaWarp || warp == kMmaWarp2) && lane == 0) {
+        // ============ MMA issuers: warp 16 the even jobs, warp 17 the odd ones ============
+        // Both walk every job of the CTA, so that both take part in every B tile change.
+        const uint32_t mine = warp == kMmaWarp ? 0u : 1u;
+        int cur_tile = -1;
+        uint32_t bphase = 0, idesc = 0, g_steps = 0, es = 0, eph = 0;
+        uint64_t bdesc_hi0 = 0, bdesc_lo0 = 0;  // k-step 0 of the current tile's B terms
+        long long t_acc = 0, t_w = 0, t_b = 0;
+        const long long t_start = tick<kProf>();
+        const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
+        const uint64_t adesc_e = ptx::smem_desc(sbase + L.e0, 32u, 128u);
+        const uint32_t e_step = (uint32_t)p.erows;  // one E stage in 16 B units
+        uint32_t jc = 0;
+        bool ok = true;
+        if (p.debug_stall) ok = ptx::mbar_wait(bars + 8 * BAR_NEVER, 0, s_abort, p.wait_limit);
+        JobIter it;
+        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
+            const int tile = it.tile;
+            if (tile != cur_tile) {
+                const long long tb = tick<kProf>();
+                // this issuer is done with the old tile once its MMAs so far are complete
+                if (cur_tile >= 0) ptx::mma_commit(bars + 8 * BAR_TILE);
+                ok = ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit);
+                bphase ^= 1;
+                if (!ok) break;
+                ptx::tc_fence_after();
+                cur_tile = tile;
+                if (kProf) t_b += tick<kProf>() - tb;
+                const TileDesc td = s_tiles[tile];
+                g_steps = (uint32_t)td.g;
+                idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
+                const uint32_t sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
+                bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
+                bdesc_lo0 = ptx::smem_desc(sbase + L.b_lo, 128u, sbo_b);
+            }
+            if ((jc & 1u) == mine) {
+                const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;  // accumulator
                 const long long t0 = tick<kProf>();
-                // start signal: phase ph of the stage's empty barrier (drained and E built);
-                // otherwise the previous phase (drained) and then E full
-                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), kStartSignal ? ph : ph ^ 1u, s_abort, p.wait_limit);
+                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
                 const long long t1 = tick<kProf>();
-                ok = ok && (kStartSignal || ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit));
+                ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
                 if (kProf) {
                     t_acc += t1 - t0;
                     t_w += tick<kProf>() - t1;
@@ -392,9 +368,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 if (!ok) break;
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem_base + s * acc_stride;
-                // A of k-step g starts 4g entries (64 B) into the E stage, B_g 256 B into each term:
-                // the descriptors' address fields (bits 0-13, in 16 B units) advance by 4 and 16
-                const uint64_t adesc0 = ptx::smem_desc(sbase + L.e0 + es * (uint32_t)p.erows * 16u, 32u, 128u);
+                // A of k-step g starts 4g entries (64 B) into the E stage, B_g 256 B into each
+                // term: the descriptors' address fields (bits 0-13, in 16 B units) advance by
+                // 4 and 16
+                const uint64_t adesc0 = adesc_e + es * e_step;
                 // D = -T (bias pieces in the last k-step of the hi term)
                 ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
                 if (kTerms == 2) {
@@ -406,116 +383,83 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     for (uint32_t g = 0; g < g_steps; ++g)
                         ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
                 }
-                if (!kStartSignal) ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));  // else by a drain thread
+                ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
             }
-            // drain: nothing may still write TMEM or shared memory when they are freed
-            ptx::mma_commit(bars + 8 * BAR_DRAIN);
-            if (!ptx::mbar_wait_drain(bars + 8 * BAR_DRAIN, dphase, p.wait_limit)) *s_abort = 1;
-            if (b_pending && !ptx::mbar_wait_drain(bars + 8 * BAR_BFULL, bphase, p.wait_limit)) *s_abort = 1;
-            if (kProf) {
-                long long *pr = p.prof + 32 * blockIdx.x;
-                pr[0] = t_acc;
-                pr[1] = t_w;
+            if (++es == (uint32_t)kEStages) {
+                es = 0;
+                eph ^= 1u;
+            }
+        }
+        // drain: nothing may still write TMEM or shared memory when they are freed
+        ptx::mma_commit(bars + 8 * (BAR_DRAIN + mine));
+        if (!ptx::mbar_wait_drain(bars + 8 * (BAR_DRAIN + mine), 0, p.wait_limit)) *s_abort = 1;
+        if (kProf) {
+            long long *pr = p.prof + 32 * blockIdx.x;
+            pr[mine] = t_acc;
+            if (mine == 0) {
                 pr[2] = t_b;
                 pr[3] = tick<kProf>() - t_start;
                 pr[10] = jc;
+                pr[11] = t_w;
             }
         }
-        __syncwarp();
-    } else if (warp >= kWWarp) {
-        // ====================== E builders (warps 17-19) ======================
-        // Thread et = 0 (warp 17, lane 0) also prefetches the code windows.
-        const int et = threadIdx.x - kWWarp * 32;
-        const uint32_t codes = sbase + L.codes;
-        JobIter ahead;  // the job whose code window is fetched next
-        ahead.init(blockIdx.x, p.n_mtiles);
-        auto fetch = [&](uint32_t jc) {  // et 0: code window of the jc-th job into its ring stage
-            if (ahead.job >= njobs) return;
-            const int64_t m = ahead.m;
-            ahead.next(gridDim.x, p.n_mtiles);
-            const uint32_t st = jc % kCodeStages;
-            const uint32_t dst = codes + st * (seq_bytes + zm_bytes);
-            ptx::mbar_arrive_expect_tx(bars + 8 * (BAR_CODE + st), seq_bytes + zm_bytes);
-            ptx::bulk_g2s(dst, p.seq2 + m * (kBM / 16), seq_bytes, bars + 8 * (BAR_CODE + st));
-            ptx::bulk_g2s(dst + seq_bytes, p.zmask + m * (kBM / 32), zm_bytes, bars + 8 * (BAR_CODE + st));
-        };
-        if (et == 0)
-            for (uint32_t j = 0; j < kCodeStages; ++j) fetch(j);
-        long long t_code = 0, t_we = 0, t_build = 0;
-        bool signal_fail = false;  // et 0 gave up waiting for the previous start signal
-        const long long t_start = tick<kProf>();
-        uint32_t jc = 0;
+    } else if (warp == kLoadWarp && lane == 0) {
+        // ============ loader: B tiles at tile changes, E windows kEStages jobs ahead ============
+        int cur_tile = -1;
+        uint32_t tphase = 0, bphase = 0, es = 0, eph = 0, jc = 0;
+        uint32_t issued[kEStages];  // per E stage: 1 + the phase of its last copy, 0 = none
+        for (int k = 0; k < kEStages; ++k) issued[k] = 0;
+        bool b_pending = false, ok = true;
+        long long t_we = 0, t_tile = 0;
         JobIter it;
         for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
             const int tile = it.tile;
-            const int g = s_tiles[tile].g;
-            const int entries = kBM + 4 * g + 2;
-            const uint32_t cs = jc % kCodeStages, cph = (jc / kCodeStages) & 1u;
-            const uint32_t s = jc % kEStages, ph = (jc / kEStages) & 1u;
-            const long long t0 = tick<kProf>();
-            bool ok = ptx::mbar_wait(bars + 8 * (BAR_CODE + cs), cph, s_abort, p.wait_limit);
-            const long long t1 = tick<kProf>();
-            ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
-            // every builder thread leaves together when any of them gave up (no one is left
-            // waiting at the barrier below)
-            if (ptx::bar_any(kEBarrier, kEWarps * 32, !ok || signal_fail)) break;
-            if (kProf) {
-                t_code += t1 - t0;
-                t_we += tick<kProf>() - t1;
-            }
-            const uint32_t *cw = reinterpret_cast<const uint32_t *>(smem + L.codes + cs * (seq_bytes + zm_bytes));
-            const uint32_t *zw = cw + seq_bytes / 4;
-            uint4 *e = reinterpret_cast<uint4 *>(smem + L.e0 + s * (uint32_t)p.erows * 16u);
-            // one-hot of a base as 4 bf16 channels in two words: 1.0 (0x3F80) in half
-            // (code & 1) of word (code >> 1); a zero-masked base gives zeros
-            auto onehot = [](uint32_t code, uint32_t zero) {
-                const uint32_t h = zero ? 0u : (0x3F80u << ((code & 1u) << 4));
-                return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
-            };
-            const long long t2 = tick<kProf>();
-            // the one-hot of base i is the first half of entry i and the second half of
-            // entry i - 1: computed once, stored twice
-            uint2 *e2 = reinterpret_cast<uint2 *>(e);
-#pragma unroll 2
-            for (int i = et; i <= entries; i += kEWarps * 32) {
-                const uint2 a = onehot((cw[i >> 4] >> (2 * (i & 15))) & 3u, (zw[i >> 5] >> (i & 31)) & 1u);
-                if (i < entries) e2[2 * i] = a;
-                if (i > 0) e2[2 * i - 1] = a;
-            }
-            // each writer makes its E entries visible to the tensor cores and orders its
-            // reads of code stage cs before the refill below
-            ptx::fence_proxy_async_smem();
-            ptx::bar_sync(kEBarrier, kEWarps * 32);
-            if (kProf) t_build += tick<kProf>() - t2;
-            if (et == 0) {
-                fetch(jc + kCodeStages);
-                if (kStartSignal) {
-                    // this arrival counts toward the job's start signal, so the stage's
-                    // previous start signal (its previous job) must have completed first
-                    const uint32_t as = jc & acc_mask, aph = (jc >> acc_shift) & 1u;
-                    if (jc >= (uint32_t)p.acc_stages)
-                        signal_fail = !ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + as), aph ^ 1u, s_abort, p.wait_limit);
-                    if (!signal_fail) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + as));
-                } else {
-                    ptx::mbar_arrive(bars + 8 * (BAR_WFULL + s));
+            const TileDesc &td = s_tiles[tile];
+            if (tile != cur_tile) {
+                if (cur_tile >= 0) {  // both issuers' MMAs on the old B are complete
+                    const long long t0 = tick<kProf>();
+                    ok = ptx::mbar_wait(bars + 8 * BAR_TILE, tphase, s_abort, p.wait_limit);
+                    tphase ^= 1;
+                    if (kProf) t_tile += tick<kProf>() - t0;
+                    if (!ok) break;
+                    // the previous B copy has landed (both issuers waited for it)
                 }
+                ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * kTerms);
+                ptx::bulk_g2s(sbase + L.b_hi, p.bbuf + td.b_off, (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
+                if (kTerms == 2)
+                    ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes, (uint32_t)td.b_bytes,
+                                  bars + 8 * BAR_BFULL);
+                b_pending = true;
+                bphase ^= 1;
+                cur_tile = tile;
+            }
+            // E window of this job: entries m0 .. m0 + 128 + 4g + 1 (16 B each)
+            const long long t0 = tick<kProf>();
+            ok = ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + es), eph ^ 1u, s_abort, p.wait_limit);
+            if (kProf) t_we += tick<kProf>() - t0;
+            if (!ok) break;
+            const uint32_t bytes = 16u * (uint32_t)(kBM + 4 * td.g + 2);
+            ptx::mbar_arrive_expect_tx(bars + 8 * (BAR_WFULL + es), bytes);
+            ptx::bulk_g2s(sbase + L.e0 + es * (uint32_t)p.erows * 16u, p.e16 + it.m * kBM, bytes,
+                          bars + 8 * (BAR_WFULL + es));
+            issued[es] = 1u + eph;
+            if (++es == (uint32_t)kEStages) {
+                es = 0;
+                eph ^= 1u;
             }
         }
-        if (kProf && et == 0) {
+        // on an abort, copies still in flight must land before the CTA frees its memory
+        if (*s_abort) {
+            for (int k = 0; k < kEStages; ++k)
+                if (issued[k]) ptx::mbar_wait_drain(bars + 8 * (BAR_WFULL + k), issued[k] - 1u, p.wait_limit);
+            if (b_pending) ptx::mbar_wait_drain(bars + 8 * BAR_BFULL, bphase ^ 1u, p.wait_limit);
+        }
+        if (kProf) {
             long long *pr = p.prof + 32 * blockIdx.x;
-            pr[4] = t_code;
-            pr[5] = t_we;
-            pr[11] = t_build;
+            pr[4] = t_we;
+            pr[5] = t_tile;
         }
-        // a prefetched window may still be in flight when the loop ends early
-        if (et == 0)
-            for (uint32_t j = jc; j < jc + kCodeStages; ++j) {
-                const long long job = blockIdx.x + (long long)j * gridDim.x;
-                if (job >= njobs || *s_abort == 0) break;
-                ptx::mbar_wait_drain(bars + 8 * (BAR_CODE + j % kCodeStages), (j / kCodeStages) & 1u,
-                                     p.wait_limit);
-            }
     } else if (warp < kEpiWarps) {
         // ===================== epilogue (warps 0-15) ======================
         const int q = warp & 3;     // TMEM lanes 32q .. 32q+31
@@ -533,8 +477,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
             if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
-            // start-signal hand-off: the job's MMAs are complete, so its E stage is free
-            if (kStartSignal && warp == 0 && lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_WEMPTY + jc % kEStages));
             const long long t1 = tick<kProf>();
             if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
@@ -617,6 +559,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             }
         }
     }
+
 
     // ---- teardown
     __syncthreads();

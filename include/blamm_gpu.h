@@ -271,9 +271,9 @@ int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, i
  * block in the allocator).  Same arguments, results and status codes as
  * blamm_scan_device, but the packed stream, candidate list, counters and
  * status word live in one fixed array of device memory that this library
- * declares (about 19 MiB per device, reserved when the library's device code
- * is loaded there).  Limits: n <= 8 Mi positions per call (more gives
- * BLAMM_ERR_ARG) and at most 2 Mi tensor-core candidates per call (more gives
+ * declares (about 73 MiB per device, reserved when the library's device code
+ * is loaded there).  Limits: n <= 4 Mi positions per call (more gives
+ * BLAMM_ERR_ARG) and at most 1 Mi tensor-core candidates per call (more gives
  * BLAMM_ERR_OVERFLOW: scan fewer positions per call).  The counters and the
  * status word are set to zero at the start of every call.
  * Preconditions: a bank (blamm_set_motifs) and, in the tensor-core modes, a

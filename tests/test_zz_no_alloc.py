@@ -13,7 +13,7 @@ from blamm_gb300._native import BLAMM_ERR_ARG, BLAMM_ERR_STATE, BlammError
 
 pytestmark = pytest.mark.gpu
 
-STATIC_MAX_BASES = 8 << 20
+STATIC_MAX_BASES = 4 << 20
 
 
 def _device_case(n: int, seed: int):
