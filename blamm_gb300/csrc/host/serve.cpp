@@ -84,11 +84,12 @@ int fail(blamm_server *s, int code, const char *fmt, ...)
     return code;
 }
 
-// Device bytes a request holds while it runs: raw and packed stream, run table,
-// candidates (at least the context's initial 1 Mi list), hits, tile plan.
+// Device bytes a request holds while it runs: raw and packed stream, its one-hot
+// entries (16 B per position), run table, candidates (at least the context's initial
+// 1 Mi list), hits, tile plan.
 int64_t request_bytes(int64_t n, int64_t nruns, int64_t cols, int p_rows)
 {
-    const int64_t stream = n + (n + 2048) / 32 * 12 + 8 * nruns;
+    const int64_t stream = n + (n + 2048) / 32 * 12 + 16 * (n + 2048) + 8 * nruns;
     const int64_t cand = 8 * std::max<int64_t>(int64_t(1) << 20, n * cols / 1000);
     const int64_t hits = 16 * std::max<int64_t>(int64_t(1) << 16, n * cols / 2000);
     const int64_t plan = cols * (int64_t)p_rows * 2 * 2 * 2 + (int64_t(1) << 20);
