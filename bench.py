@@ -587,6 +587,7 @@ def run_ours(a, rank, world, local):
         t1 = time.perf_counter()
         e2e_step()
         e2e_t.append(time.perf_counter() - t1)
+    e2e_st = sc.stats()
     e2e_digest = hit_digest(hh[: nhc.value * HIT_DTYPE.itemsize].numpy().view(HIT_DTYPE))
     e2e_value = total_units / float(np.mean(e2e_t)) if world == 1 else units / float(np.mean(e2e_t)) * world
 
@@ -645,6 +646,7 @@ def run_ours(a, rank, world, local):
         "wall_s_timed_region": wall,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n + 8 * len(runs)),
                 "d2h_bytes_per_step": int(16 * nhc.value + 8), "ms_per_step": 1e3 * float(np.mean(e2e_t)),
+                "call_kernel_ms": float(e2e_st["kernel_ms"]), "call_total_ms": float(e2e_st["total_ms"]),
                 "same_hits": e2e_digest == ref_digest},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -92,6 +93,18 @@ struct blamm_ctx {
     int64_t hits_cap = 0;
     unsigned long long *d_counters = nullptr;  // [0] candidates, [1] hits
     int *d_status = nullptr;
+    // hit filtering of one chunk of a pipelined blamm_scan: hits at chunk positions >=
+    // keep_below are dropped (0: none), pos_base is added to the positions written
+    int64_t keep_below = 0, pos_base = 0;
+    // blamm_scan's copy pipeline: a second stream and double-buffered chunk inputs
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[2] = {nullptr, nullptr};
+    char *d_chunk_bases[2] = {nullptr, nullptr};
+    size_t cap_chunk_bases[2] = {0, 0};
+    int64_t *d_chunk_runs[2] = {nullptr, nullptr};
+    size_t cap_chunk_runs[2] = {0, 0};
+    int64_t *h_chunk_runs[2] = {nullptr, nullptr};  // pinned: their copies stay asynchronous
+    size_t cap_h_chunk_runs = 0;
     bool prof_on = false;
     long long *d_prof = nullptr;
     std::vector<long long> prof;  // last scan's role timing, 32 counters per CTA
@@ -441,11 +454,18 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
     void *bufs[] = {ctx->d_P,      ctx->d_len,   ctx->d_thr,      ctx->d_tiles, ctx->d_bbuf,
                     ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask, ctx->d_e16,
                     ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status,
-                    ctx->d_active};
+                    ctx->d_active, ctx->d_chunk_bases[0], ctx->d_chunk_bases[1], ctx->d_chunk_runs[0],
+                    ctx->d_chunk_runs[1]};
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     for (void *b : bufs)
         if (b) cudaFree(b);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : ctx->chunk_ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto &h : ctx->h_chunk_runs)
+        if (h) cudaFreeHost(h);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -717,6 +737,8 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     r.hits = d_hits;
     r.hit_count = ctx->d_counters + 1;
     r.hit_cap = hit_cap;
+    r.keep_below = ctx->keep_below;
+    r.pos_base = ctx->pos_base;
     const int64_t nc = ctx->stats.candidates;
     if (nc > 0) {
         const int threads = 256;
@@ -751,6 +773,8 @@ static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t n
     p.hits = d_hits;
     p.hit_count = ctx->d_counters + 1;
     p.hit_cap = hit_cap;
+    p.keep_below = ctx->keep_below;
+    p.pos_base = ctx->pos_base;
     const int threads = 256;
     int cpb = 32;
     while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
@@ -818,6 +842,104 @@ int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n, const int6
     return scan_core(ctx, d_bases, n, d_run_start, nruns, d_hits, hit_cap, n_hits);
 }
 
+// blamm_scan on a long stream: chunks of kPipeChunk positions (plus the longest motif - 1
+// bases of overlap, whose window starts belong to the next chunk), each chunk's bases
+// copied in on a second stream while the previous chunk is scanned, and its hits copied
+// out there while the next one is scanned.
+constexpr int64_t kPipeChunk = int64_t(16) << 20;
+
+static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                               int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
+{
+    const int64_t ov = std::max(ctx->lmax - 1, 0);
+    const int64_t nchunks = (n + kPipeChunk - 1) / kPipeChunk;
+    int rc = BLAMM_OK;
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = ensure(ctx, &ctx->d_chunk_bases[b], &ctx->cap_chunk_bases[b], (size_t)(kPipeChunk + ov))))
+            return rc;
+        if ((rc = ensure(ctx, &ctx->d_chunk_runs[b], &ctx->cap_chunk_runs[b], (size_t)nruns + 1))) return rc;
+    }
+    size_t hc = (size_t)ctx->hits_cap;
+    if ((rc = ensure(ctx, &ctx->d_hits, &hc, (size_t)std::max<int64_t>(hit_cap, 1)))) return rc;
+    ctx->hits_cap = (int64_t)hc;
+    if (!ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (auto &ev : ctx->chunk_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));  // the buffers exist before the copy stream uses them
+    if (ctx->cap_h_chunk_runs < (size_t)nruns + 1) {
+        for (auto &h : ctx->h_chunk_runs) {
+            if (h) CK(cudaFreeHost(h));
+            h = nullptr;
+        }
+        ctx->cap_h_chunk_runs = 0;
+        for (auto &h : ctx->h_chunk_runs) CK(cudaHostAlloc((void **)&h, sizeof(int64_t) * ((size_t)nruns + 1), 0));
+        ctx->cap_h_chunk_runs = (size_t)nruns + 1;
+    }
+    int64_t kruns[2] = {0, 0};  // per buffer: run starts of its chunk (in h_chunk_runs)
+    auto issue_in = [&](int64_t k) -> int {
+        const int b = (int)(k & 1);
+        const int64_t c0 = k * kPipeChunk, end = std::min(n, c0 + kPipeChunk + ov);
+        int64_t *hr = ctx->h_chunk_runs[b];  // its previous copy (chunk k - 2) has landed
+        int64_t m = 0;
+        hr[m++] = 0;  // c0 lies inside some run
+        for (const int64_t *r = std::upper_bound(run_start, run_start + nruns, c0); r < run_start + nruns && *r < end;
+             ++r)
+            hr[m++] = *r - c0;
+        kruns[b] = m;
+        CK(cudaMemcpyAsync(ctx->d_chunk_bases[b], bases + c0, (size_t)(end - c0), cudaMemcpyHostToDevice,
+                           ctx->copy_stream));
+        CK(cudaMemcpyAsync(ctx->d_chunk_runs[b], hr, sizeof(int64_t) * (size_t)m, cudaMemcpyHostToDevice,
+                           ctx->copy_stream));
+        CK(cudaEventRecord(ctx->chunk_ev[b], ctx->copy_stream));
+        return BLAMM_OK;
+    };
+    auto finish = [&](int code) {
+        ctx->keep_below = ctx->pos_base = 0;
+        cudaStreamSynchronize(ctx->copy_stream);
+        return code;
+    };
+    blamm_stats total{};
+    total.positions = n;
+    int64_t nh_total = 0;
+    if ((rc = issue_in(0))) return finish(rc);
+    for (int64_t k = 0; k < nchunks; ++k) {
+        const int b = (int)(k & 1);
+        // the next chunk's input buffer served chunk k - 1, whose scan has returned
+        if (k + 1 < nchunks && (rc = issue_in(k + 1))) return finish(rc);
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->chunk_ev[b], 0));
+        const int64_t c0 = k * kPipeChunk, c1 = std::min(n, c0 + kPipeChunk), end = std::min(n, c1 + ov);
+        ctx->keep_below = end > c1 ? c1 - c0 : 0;
+        ctx->pos_base = c0;
+        const int64_t at = std::min(nh_total, hit_cap), cap_k = hit_cap - at;
+        int64_t nh = 0;
+        rc = scan_core(ctx, ctx->d_chunk_bases[b], end - c0, ctx->d_chunk_runs[b], kruns[b], ctx->d_hits + at,
+                       cap_k, &nh);
+        if (rc && rc != BLAMM_ERR_OVERFLOW) return finish(rc);
+        // scan_core returned after its stream drained: copy this chunk's hits out beside the next scan
+        const int64_t ncopy = std::min(nh, cap_k);
+        if (ncopy > 0)
+            CK(cudaMemcpyAsync(hits + at, ctx->d_hits + at, sizeof(blamm_hit) * ncopy, cudaMemcpyDeviceToHost,
+                               ctx->copy_stream));
+        nh_total += nh;
+        total.columns = ctx->stats.columns;
+        total.candidates += ctx->stats.candidates;
+        total.tiles = ctx->stats.tiles;
+        total.launches += ctx->stats.launches;
+        total.kernel_ms += ctx->stats.kernel_ms;
+        total.scan_ms += ctx->stats.scan_ms;
+        total.rescore_ms += ctx->stats.rescore_ms;
+    }
+    finish(BLAMM_OK);
+    CK(cudaGetLastError());
+    total.hits = nh_total;
+    ctx->stats = total;
+    *n_hits = nh_total;
+    return nh_total > hit_cap
+               ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld", (long long)nh_total, (long long)hit_cap)
+               : BLAMM_OK;
+}
+
 int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start, int64_t nruns,
                blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
 {
@@ -831,6 +953,14 @@ int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_
         if (run_start[r] <= run_start[r - 1] || run_start[r] >= n)
             return fail(ctx, BLAMM_ERR_ARG, "run_start must ascend strictly inside [0, n)");
     CK(cudaSetDevice(ctx->device));
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    if (n > 2 * kPipeChunk) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const int rc = scan_host_pipelined(ctx, bases, n, run_start, nruns, hits, hit_cap, n_hits);
+        ctx->stats.total_ms =
+            std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    }
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
     if (rc) return rc;

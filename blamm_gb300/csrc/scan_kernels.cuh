@@ -116,6 +116,8 @@ struct PlainParams {
     void *hits;  // blamm_hit*
     unsigned long long *hit_count;
     int64_t hit_cap;
+    int64_t keep_below;  // hits at positions >= keep_below are dropped (0: none are)
+    int64_t pos_base;    // added to the positions written
 };
 
 struct HitRec {
@@ -187,10 +189,10 @@ __global__ void __launch_bounds__(256) scan_plain_kernel(PlainParams p)
                 int b = code[j];
                 if (b < 4) s = __fadd_rn(s, col[4 * j + b]);
             }
-            hit = s >= sThr[cc];
+            hit = s >= sThr[cc] && (p.keep_below == 0 || pos < p.keep_below);
         }
-        emit_hits_warp(hit, pos, p.cols ? p.cols[c0 + cc] : c0 + cc, s, reinterpret_cast<HitRec *>(p.hits),
-                       p.hit_count, p.hit_cap);
+        emit_hits_warp(hit, pos + p.pos_base, p.cols ? p.cols[c0 + cc] : c0 + cc, s,
+                       reinterpret_cast<HitRec *>(p.hits), p.hit_count, p.hit_cap);
     }
 }
 
@@ -274,6 +276,8 @@ struct RescoreParams {
     void *hits;
     unsigned long long *hit_count;
     int64_t hit_cap;
+    int64_t keep_below;  // hits at positions >= keep_below are dropped (0: none are)
+    int64_t pos_base;    // added to the positions written
 };
 
 __global__ void __launch_bounds__(256) rescore_kernel(RescoreParams p)
@@ -299,10 +303,10 @@ __global__ void __launch_bounds__(256) rescore_kernel(RescoreParams p)
                     int b = base_code_at(p.seq2, p.zmask, pos + j);
                     if (b < 4) s = __fadd_rn(s, __ldg(pc + 4 * j + b));
                 }
-                hit = s >= __ldg(p.thr + col);
+                hit = s >= __ldg(p.thr + col) && (p.keep_below == 0 || pos < p.keep_below);
             }
         }
-        emit_hits_warp(hit, pos, col, s, reinterpret_cast<HitRec *>(p.hits), p.hit_count,
+        emit_hits_warp(hit, pos + p.pos_base, col, s, reinterpret_cast<HitRec *>(p.hits), p.hit_count,
                        p.hit_cap);
     }
 }

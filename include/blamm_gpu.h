@@ -68,7 +68,8 @@ typedef struct {
     int32_t tiles;       /* motif tiles (tcgen05 N tiles) */
     int32_t launches;    /* kernels launched by the last scan */
     float kernel_ms;     /* device time of all kernels of the call (CUDA events) */
-    float total_ms;      /* device time of the whole call incl. copies */
+    float total_ms;      /* time of the whole call incl. copies (device events; wall time
+                            when blamm_scan pipelines a long stream in chunks) */
     float scan_ms;       /* device time of the scan kernel alone (tcgen05 or plain FP32) */
     float rescore_ms;    /* device time of the rescoring kernel (tcgen05 modes) */
 } blamm_stats;
@@ -115,7 +116,12 @@ int blamm_set_columns(blamm_ctx *ctx, const int32_t *cols, int n);
  *   maximal contiguous run (the SeqBlock markers, src/sequence.cpp:81-88).
  *   A window that crosses into the next run is not a hit (src/pwmscan.cpp:122-126).
  * Writes up to hit_cap hits (unordered) and their number to *n_hits.
- * Returns BLAMM_ERR_OVERFLOW, with *n_hits = the total, when hit_cap is too small. */
+ * Returns BLAMM_ERR_OVERFLOW, with *n_hits = the total, when hit_cap is too small.
+ * A stream longer than 32 Mi positions is scanned in chunks of 16 Mi positions
+ * (plus the longest motif - 1 bases of overlap): each chunk's bases are copied
+ * in on a second stream while the previous chunk is scanned, and its hits are
+ * copied out while the next one is scanned (pinned host buffers let the copies
+ * run beside the scan). */
 int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
                int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits);
 

@@ -172,3 +172,33 @@ def test_many_short_sequences_one_call_equals_one_call_each(scanner):
         mine["pos"] -= starts[i]
         ok, msg = same_hits(mine, alone)
         assert ok, f"sequence {i}: {msg}"
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_pipelined_host_scan_equals_device_scan(mode):
+    """blamm_scan on a stream longer than two pipeline chunks (16 Mi positions each, copies on
+    a second stream) gives the hit set of one device-resident scan, with runs that start just
+    before, at and just after the chunk boundaries and inside the overlap."""
+    torch = _torch()
+    from blamm_gb300 import GpuScanner
+    P, lens, thr = make_bank(71, 48, 5, 30, rel=0.86)
+    n = 40_000_000
+    bases, runs = make_stream(72, n, nruns=40, lower_frac=0.002)
+    chunk = 16 << 20
+    extra = [chunk - 3, chunk, chunk + 2, chunk + 17, 2 * chunk - 1, 2 * chunk + 5]
+    runs = np.unique(np.concatenate([runs, np.array(extra, dtype=np.int64)]))
+    sc = GpuScanner(0, mode)
+    try:
+        sc.set_motifs(P, lens, thr)
+        got = sc.scan(bases, runs)
+        d_b = torch.from_numpy(bases).cuda()
+        d_r = torch.from_numpy(runs).cuda()
+        cap = len(got) + 4096
+        d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+        want = _hits(d_h, nh)
+        assert len(got) > 10_000
+        ok, msg = same_hits(got, want)
+        assert ok, msg
+    finally:
+        sc.close()
