@@ -33,6 +33,27 @@ __device__ __forceinline__ int base_code_at(const uint32_t *seq2, const uint32_t
     return z ? 4 : (int)b;
 }
 
+// Sequential FP32 score of the window at pos (motif position order, __fadd_rn: the
+// reference's sum), zero-masked bases adding nothing.  The 2-bit codes and mask bits of
+// 16 positions come from two words of each array (the padded stream covers the reads).
+__device__ __forceinline__ float window_score(const uint32_t *seq2, const uint32_t *zmask, const float *pc,
+                                              int64_t pos, int L)
+{
+    float s = 0.0f;
+    for (int j = 0; j < L; j += 16) {
+        const int64_t q = pos + j;
+        const int64_t w = q >> 4, wz = q >> 5;
+        const uint64_t cw = (uint64_t)__ldg(seq2 + w) | ((uint64_t)__ldg(seq2 + w + 1) << 32);
+        const uint64_t zw = (uint64_t)__ldg(zmask + wz) | ((uint64_t)__ldg(zmask + wz + 1) << 32);
+        const uint32_t codes = (uint32_t)(cw >> (2 * (q & 15)));
+        const uint32_t zero = (uint32_t)(zw >> (q & 31));
+        const int cnt = min(16, L - j);
+        for (int k = 0; k < cnt; ++k)
+            if (!((zero >> k) & 1u)) s = __fadd_rn(s, __ldg(pc + 4 * (j + k) + ((codes >> (2 * k)) & 3u)));
+    }
+    return s;
+}
+
 // end (exclusive) of the run that contains position p
 __device__ __forceinline__ int64_t run_end_of(const int64_t *run_start, int64_t nruns, int64_t n,
                                               int64_t p)
@@ -298,11 +319,7 @@ __global__ void __launch_bounds__(256) rescore_kernel(RescoreParams p)
             col = __ldg(p.slot_col + (int32_t)(c & ((1u << kColBits) - 1u)));
             const int L = __ldg(p.col_len + col);
             if (pos + L <= run_end_of(p.run_start, p.nruns, p.n, pos)) {
-                const float *pc = p.P + (size_t)col * p.p_rows;
-                for (int j = 0; j < L; ++j) {
-                    int b = base_code_at(p.seq2, p.zmask, pos + j);
-                    if (b < 4) s = __fadd_rn(s, __ldg(pc + 4 * j + b));
-                }
+                s = window_score(p.seq2, p.zmask, p.P + (size_t)col * p.p_rows, pos, L);
                 hit = s >= __ldg(p.thr + col) && (p.keep_below == 0 || pos < p.keep_below);
             }
         }
