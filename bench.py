@@ -589,7 +589,10 @@ def run_ours(a, rank, world, local):
         e2e_t.append(time.perf_counter() - t1)
     e2e_st = sc.stats()
     e2e_digest = hit_digest(hh[: nhc.value * HIT_DTYPE.itemsize].numpy().view(HIT_DTYPE))
-    e2e_value = total_units / float(np.mean(e2e_t)) if world == 1 else units / float(np.mean(e2e_t)) * world
+    # median over the steps: a single host-side stall (seen now and then on the pinned copies)
+    # would otherwise dominate the mean of a few steps; the mean and the maximum are reported too
+    e2e_med = float(np.median(e2e_t))
+    e2e_value = total_units / e2e_med if world == 1 else units / e2e_med * world
 
     # ---- other modes on the same stream (same hits required)
     modes = {}
@@ -645,7 +648,9 @@ def run_ours(a, rank, world, local):
         "scan_kernel_ms": kern_ms, "rescore_kernel_ms": float(st["rescore_ms"]),
         "wall_s_timed_region": wall,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n + 8 * len(runs)),
-                "d2h_bytes_per_step": int(16 * nhc.value + 8), "ms_per_step": 1e3 * float(np.mean(e2e_t)),
+                "d2h_bytes_per_step": int(16 * nhc.value + 8), "ms_per_step": 1e3 * e2e_med,
+                "stat": f"median of {len(e2e_t)} calls", "ms_per_step_mean": 1e3 * float(np.mean(e2e_t)),
+                "ms_per_step_max": 1e3 * float(np.max(e2e_t)),
                 "call_kernel_ms": float(e2e_st["kernel_ms"]), "call_total_ms": float(e2e_st["total_ms"]),
                 "same_hits": e2e_digest == ref_digest},
         "gpu_launches": int(launches),
