@@ -2,7 +2,7 @@
 // one persistent CTA per SM.
 //
 // Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
-// The packing kernel writes one 16-byte entry per stream position,
+// After packing, e16_kernel writes one 16-byte entry per stream position,
 // E[i] = onehot(base i) ++ onehot(base i+1) (2 bases x 4 channels x bf16).
 // For an M tile of 128 positions starting at m0, a bulk copy brings entries
 // m0 .. m0+128+4g+1 into shared memory; read with row stride 16 B, 8-row group

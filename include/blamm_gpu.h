@@ -254,12 +254,13 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
 int blamm_guard_band(const blamm_ctx *ctx, float *out);
 /* Role timing of the tensor-core scan kernel: enable (1) / disable (0) it for
  * later scans; read the last scan's counters (32 int64 per CTA, clock cycles:
- * 0 MMA waits for a free accumulator, 1 MMA waits for E, 2 B-tile reloads,
- * 3 MMA loop, 4 E-builder waits for a code window, 5 E-builder waits for a
- * free E stage, 6 epilogue hand-back, 7 epilogue waits for an accumulator,
- * 8 epilogue loop, 9 epilogue drain, 10 jobs, 11 E build, 12 epilogue rounds with
- * candidates, 13 TMEM loads, 14 fence after the wait, 15 sign test and staging,
- * 16-23 drain of epilogue warps 0-7, 24-31 their waits).  *nctas receives the
+ * 0 / 1 the even / odd issuer's waits for a free accumulator, 2 issuers' waits
+ * for B tiles, 3 MMA loop, 4 loader waits for a free E stage, 5 loader waits at
+ * tile changes, 6 epilogue hand-back, 7 epilogue waits for an accumulator,
+ * 8 epilogue loop, 9 epilogue drain, 10 jobs, 11 even issuer's waits for E
+ * windows, 12 epilogue rounds with candidates, 13 TMEM loads, 14 fence after the
+ * wait, 15 candidate test and staging, 16-23 drain of epilogue warps 0-7, 24-31
+ * their waits).  *nctas receives the
  * CTA count.  The timing variant of the kernel is slower than the scan itself. */
 int blamm_debug_profile(blamm_ctx *ctx, int enable);
 /* Failure-path test hook: with enable = 1 the tensor-core scan kernel first
