@@ -202,3 +202,26 @@ def test_pipelined_host_scan_equals_device_scan(mode):
         assert ok, msg
     finally:
         sc.close()
+
+
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+def test_role_timing_instance_keeps_the_hit_set(scanner, mode):
+    """The role-timing instance of the scan kernel (blamm_debug_profile) finds the same hits
+    and fills its counters: every job of every CTA counted once."""
+    P, lens, thr = make_bank(91, 64, 5, 30, rel=0.85)
+    bases, runs = make_stream(92, 2_000_000, nruns=7)
+    scanner.set_mode(mode)
+    scanner.set_motifs(P, lens, thr)
+    want = scanner.scan(bases, runs)
+    scanner.profile(True)
+    try:
+        got = scanner.scan(bases, runs)
+        prof = scanner.profile_read()
+    finally:
+        scanner.profile(False)
+    ok, msg = same_hits(got, want)
+    assert ok, msg
+    st = scanner.stats()
+    jobs = st["tiles"] * ((len(bases) + 127) // 128)
+    assert 0 < prof.shape[0] <= jobs and int(prof[:, 10].sum()) == jobs
+    assert (prof[:, 3] > 0).all()  # the issuers' loop time
