@@ -848,8 +848,8 @@ int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n, const int6
 // out there while the next one is scanned.
 constexpr int64_t kPipeChunk = int64_t(16) << 20;
 
-static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
-                               int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
+static int scan_host_pipelined_steps(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                                     int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
 {
     const int64_t ov = std::max(ctx->lmax - 1, 0);
     const int64_t nchunks = (n + kPipeChunk - 1) / kPipeChunk;
@@ -894,19 +894,14 @@ static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, con
         CK(cudaEventRecord(ctx->chunk_ev[b], ctx->copy_stream));
         return BLAMM_OK;
     };
-    auto finish = [&](int code) {
-        ctx->keep_below = ctx->pos_base = 0;
-        cudaStreamSynchronize(ctx->copy_stream);
-        return code;
-    };
     blamm_stats total{};
     total.positions = n;
     int64_t nh_total = 0;
-    if ((rc = issue_in(0))) return finish(rc);
+    if ((rc = issue_in(0))) return rc;
     for (int64_t k = 0; k < nchunks; ++k) {
         const int b = (int)(k & 1);
         // the next chunk's input buffer served chunk k - 1, whose scan has returned
-        if (k + 1 < nchunks && (rc = issue_in(k + 1))) return finish(rc);
+        if (k + 1 < nchunks && (rc = issue_in(k + 1))) return rc;
         CK(cudaStreamWaitEvent(ctx->stream, ctx->chunk_ev[b], 0));
         const int64_t c0 = k * kPipeChunk, c1 = std::min(n, c0 + kPipeChunk), end = std::min(n, c1 + ov);
         ctx->keep_below = end > c1 ? c1 - c0 : 0;
@@ -915,7 +910,7 @@ static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, con
         int64_t nh = 0;
         rc = scan_core(ctx, ctx->d_chunk_bases[b], end - c0, ctx->d_chunk_runs[b], kruns[b], ctx->d_hits + at,
                        cap_k, &nh);
-        if (rc && rc != BLAMM_ERR_OVERFLOW) return finish(rc);
+        if (rc && rc != BLAMM_ERR_OVERFLOW) return rc;
         // scan_core returned after its stream drained: copy this chunk's hits out beside the next scan
         const int64_t ncopy = std::min(nh, cap_k);
         if (ncopy > 0)
@@ -930,14 +925,24 @@ static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, con
         total.scan_ms += ctx->stats.scan_ms;
         total.rescore_ms += ctx->stats.rescore_ms;
     }
-    finish(BLAMM_OK);
-    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->copy_stream));  // the hits are in host memory
     total.hits = nh_total;
     ctx->stats = total;
     *n_hits = nh_total;
     return nh_total > hit_cap
                ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld", (long long)nh_total, (long long)hit_cap)
                : BLAMM_OK;
+}
+
+// Whatever way the steps end, the chunk filter is reset and no copy into the caller's
+// buffers is still in flight.
+static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                               int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
+{
+    const int rc = scan_host_pipelined_steps(ctx, bases, n, run_start, nruns, hits, hit_cap, n_hits);
+    ctx->keep_below = ctx->pos_base = 0;
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    return rc;
 }
 
 int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start, int64_t nruns,
