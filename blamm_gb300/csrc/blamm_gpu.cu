@@ -105,6 +105,9 @@ struct blamm_ctx {
     size_t cap_chunk_runs[2] = {0, 0};
     int64_t *h_chunk_runs[2] = {nullptr, nullptr};  // pinned: their copies stay asynchronous
     size_t cap_h_chunk_runs = 0;
+    cudaEvent_t done_ev[2] = {nullptr, nullptr};  // per input buffer: its chunk's kernels are done
+    unsigned long long *h_chunk_counts = nullptr;  // pinned, 4 per chunk: candidates, hits, status
+    size_t cap_h_chunk_counts = 0;
     bool prof_on = false;
     long long *d_prof = nullptr;
     std::vector<long long> prof;  // last scan's role timing, 32 counters per CTA
@@ -463,8 +466,11 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
         if (ev) cudaEventDestroy(ev);
     for (auto &ev : ctx->chunk_ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : ctx->done_ev)
+        if (ev) cudaEventDestroy(ev);
     for (auto &h : ctx->h_chunk_runs)
         if (h) cudaFreeHost(h);
+    if (ctx->h_chunk_counts) cudaFreeHost(ctx->h_chunk_counts);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -934,14 +940,253 @@ static int scan_host_pipelined_steps(blamm_ctx *ctx, const char *bases, int64_t 
                : BLAMM_OK;
 }
 
+// One chunk's kernels, enqueued without host synchronisation (the blamm_scan_enqueue
+// sequence): candidates beyond the candidate buffer are only counted, and the rescoring
+// reads their number on the device.
+static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_runs, int64_t nruns,
+                         blamm_hit *d_hits, int64_t hit_cap)
+{
+    unsigned long long *cnt = ctx->d_counters;  // [0] candidates of this chunk, [1] hits of the call
+    const int64_t nwords32 = (n + kStreamPad + 31) / 32;
+    pack_kernel<<<(unsigned)((nwords32 + 255) / 256), 256, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
+                                                                          nwords32, ctx->lower_scores);
+    CK(cudaGetLastError());
+    if (ctx->mode == BLAMM_MODE_FP32) {
+        PlainParams p{};
+        p.seq2 = ctx->d_seq2;
+        p.zmask = ctx->d_zmask;
+        p.n = n;
+        p.run_start = d_runs;
+        p.nruns = nruns;
+        p.P = ctx->d_P;
+        p.p_rows = ctx->p_rows;
+        p.ncols = scanned_columns(ctx);
+        p.lmax = ctx->lmax;
+        p.col_len = ctx->d_len;
+        p.thr = ctx->d_thr;
+        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
+        p.hits = d_hits;
+        p.hit_count = cnt + 1;
+        p.hit_cap = hit_cap;
+        p.keep_below = ctx->keep_below;
+        p.pos_base = ctx->pos_base;
+        const int threads = 256;
+        int cpb = 32;
+        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
+        p.cols_per_block = cpb;
+        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
+        const int64_t bx = (n + threads - 1) / threads;
+        const int by = (p.ncols + cpb - 1) / cpb;
+        if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
+        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
+        CK(cudaGetLastError());
+        return BLAMM_OK;
+    }
+    launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
+    const int64_t n_mtiles = (n + kBM - 1) / kBM;
+    const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
+    if ((int)L.total > ctx->max_smem)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
+    TcParams p = tc_params(ctx, ctx->d_e16, n);
+    p.cand = ctx->d_cand;
+    p.cand_count = cnt;
+    p.cand_cap = ctx->cand_cap;
+    p.status = ctx->d_status;
+    p.wait_limit = ctx->wait_limit;
+    p.dump_ncols = ctx->ncols;
+    const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
+    launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
+    CK(cudaGetLastError());
+    RescoreParams r{};
+    r.cand = ctx->d_cand;
+    r.slot_col = ctx->d_slot_col;
+    r.cand_count = cnt;
+    r.cand_cap = ctx->cand_cap;
+    r.seq2 = ctx->d_seq2;
+    r.zmask = ctx->d_zmask;
+    r.n = n;
+    r.run_start = d_runs;
+    r.nruns = nruns;
+    r.P = ctx->d_P;
+    r.p_rows = ctx->p_rows;
+    r.col_len = ctx->d_len;
+    r.thr = ctx->d_thr;
+    r.hits = d_hits;
+    r.hit_count = cnt + 1;
+    r.hit_cap = hit_cap;
+    r.keep_below = ctx->keep_below;
+    r.pos_base = ctx->pos_base;
+    rescore_kernel<<<(unsigned)(ctx->sm_count * 8), 256, 0, ctx->stream>>>(r);
+    CK(cudaGetLastError());
+    return BLAMM_OK;
+}
+
+// The copy pipeline without host synchronisation inside a chunk: the host only waits for
+// chunk k - 1 to finish (while chunk k runs) to learn how many hits to copy out.  Returns
+// BLAMM_ERR_OVERFLOW with *cand_overflow set when a chunk had more candidates than the
+// candidate buffer holds (its hits are then incomplete: the caller rescans).
+static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                                 int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits,
+                                 int64_t *cand_overflow)
+{
+    *cand_overflow = 0;
+    const int64_t ov = std::max(ctx->lmax - 1, 0);
+    const int64_t nchunks = (n + kPipeChunk - 1) / kPipeChunk;
+    const int64_t span = kPipeChunk + ov;  // positions of the longest chunk
+    const bool tc = ctx->mode != BLAMM_MODE_FP32;
+    int rc = BLAMM_OK;
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = ensure(ctx, &ctx->d_chunk_bases[b], &ctx->cap_chunk_bases[b], (size_t)span))) return rc;
+        if ((rc = ensure(ctx, &ctx->d_chunk_runs[b], &ctx->cap_chunk_runs[b], (size_t)nruns + 1))) return rc;
+    }
+    const int64_t nwords32 = (span + kStreamPad + 31) / 32;
+    if ((rc = ensure(ctx, &ctx->d_seq2, &ctx->cap_words32, (size_t)(2 * nwords32)))) return rc;
+    if ((rc = ensure(ctx, &ctx->d_zmask, &ctx->cap_zmask, (size_t)nwords32))) return rc;
+    if (tc) {
+        if ((rc = ensure_plan(ctx))) return rc;
+        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(span)))) return rc;
+        // candidates: four times the usual first guess for a chunk (a chunk that still
+        // overflows sends the whole call to the synchronous path)
+        const double want = std::min(std::max((double)span * scanned_columns(ctx) / 250.0, (double)(1 << 20)),
+                                     512.0 * 1024 * 1024);
+        if ((double)ctx->cand_cap < want) {
+            size_t cap = ctx->cand_cap > 0 ? (size_t)ctx->cand_cap : 0;
+            if ((rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)want))) return rc;
+            ctx->cand_cap = (int64_t)cap;
+        }
+    }
+    size_t hc = (size_t)ctx->hits_cap;
+    if ((rc = ensure(ctx, &ctx->d_hits, &hc, (size_t)std::max<int64_t>(hit_cap, 1)))) return rc;
+    ctx->hits_cap = (int64_t)hc;
+    if (!ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (auto &ev : ctx->chunk_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    if (!ctx->done_ev[0])
+        for (auto &ev : ctx->done_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    if (ctx->cap_h_chunk_runs < (size_t)nruns + 1) {
+        for (auto &h : ctx->h_chunk_runs) {
+            if (h) CK(cudaFreeHost(h));
+            h = nullptr;
+        }
+        ctx->cap_h_chunk_runs = 0;
+        for (auto &h : ctx->h_chunk_runs) CK(cudaHostAlloc((void **)&h, sizeof(int64_t) * ((size_t)nruns + 1), 0));
+        ctx->cap_h_chunk_runs = (size_t)nruns + 1;
+    }
+    if (ctx->cap_h_chunk_counts < (size_t)(4 * nchunks)) {
+        if (ctx->h_chunk_counts) CK(cudaFreeHost(ctx->h_chunk_counts));
+        ctx->h_chunk_counts = nullptr;
+        ctx->cap_h_chunk_counts = 0;
+        CK(cudaHostAlloc((void **)&ctx->h_chunk_counts, sizeof(unsigned long long) * 4 * (size_t)nchunks, 0));
+        ctx->cap_h_chunk_counts = (size_t)(4 * nchunks);
+    }
+    CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the buffers exist before the copy stream uses them
+    int64_t kruns[2] = {0, 0};
+    auto issue_in = [&](int64_t k) -> int {
+        const int b = (int)(k & 1);
+        const int64_t c0 = k * kPipeChunk, end = std::min(n, c0 + kPipeChunk + ov);
+        // the staging and device buffers served chunk k - 2: its run copy has landed, and the
+        // copy stream waits for its kernels (packing reads the bases, the scans the runs)
+        if (k >= 2) {
+            CK(cudaEventSynchronize(ctx->chunk_ev[b]));
+            CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->done_ev[b], 0));
+        }
+        int64_t *hr = ctx->h_chunk_runs[b];
+        int64_t m = 0;
+        hr[m++] = 0;  // c0 lies inside some run
+        for (const int64_t *r = std::upper_bound(run_start, run_start + nruns, c0); r < run_start + nruns && *r < end;
+             ++r)
+            hr[m++] = *r - c0;
+        kruns[b] = m;
+        CK(cudaMemcpyAsync(ctx->d_chunk_bases[b], bases + c0, (size_t)(end - c0), cudaMemcpyHostToDevice,
+                           ctx->copy_stream));
+        CK(cudaMemcpyAsync(ctx->d_chunk_runs[b], hr, sizeof(int64_t) * (size_t)m, cudaMemcpyHostToDevice,
+                           ctx->copy_stream));
+        CK(cudaEventRecord(ctx->chunk_ev[b], ctx->copy_stream));
+        return BLAMM_OK;
+    };
+    unsigned long long *hc_k = ctx->h_chunk_counts;
+    int64_t copied = 0;  // hits already sent to host memory
+    // copy out the hits chunk k added, once it has finished (the host waits for that chunk)
+    auto drain_out = [&](int64_t k) -> int {
+        CK(cudaEventSynchronize(ctx->done_ev[k & 1]));
+        const int64_t upto = std::min<int64_t>((int64_t)hc_k[4 * k + 1], hit_cap);
+        if (upto > copied) {
+            CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->done_ev[k & 1], 0));
+            CK(cudaMemcpyAsync(hits + copied, ctx->d_hits + copied, sizeof(blamm_hit) * (size_t)(upto - copied),
+                               cudaMemcpyDeviceToHost, ctx->copy_stream));
+            copied = upto;
+        }
+        return BLAMM_OK;
+    };
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    if ((rc = issue_in(0))) return rc;
+    for (int64_t k = 0; k < nchunks; ++k) {
+        const int b = (int)(k & 1);
+        if (k + 1 < nchunks && (rc = issue_in(k + 1))) return rc;
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->chunk_ev[b], 0));
+        const int64_t c0 = k * kPipeChunk, c1 = std::min(n, c0 + kPipeChunk), end = std::min(n, c1 + ov);
+        ctx->keep_below = end > c1 ? c1 - c0 : 0;
+        ctx->pos_base = c0;
+        rc = enqueue_chunk(ctx, ctx->d_chunk_bases[b], end - c0, ctx->d_chunk_runs[b], kruns[b], ctx->d_hits,
+                           hit_cap);
+        ctx->keep_below = ctx->pos_base = 0;
+        if (rc) return rc;
+        // this chunk's candidate count, the running hit count and the status, to host memory
+        CK(cudaMemcpyAsync(hc_k + 4 * k, ctx->d_counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(hc_k + 4 * k + 2, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaEventRecord(ctx->done_ev[b], ctx->stream));
+        if (k >= 1 && (rc = drain_out(k - 1))) return rc;
+    }
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if ((rc = drain_out(nchunks - 1))) return rc;
+    CK(cudaStreamSynchronize(ctx->copy_stream));  // the hits are in host memory
+    blamm_stats total{};
+    total.positions = n;
+    total.columns = scanned_columns(ctx);
+    total.tiles = (int32_t)(tc ? ctx->tiles.size() : 0);
+    total.launches = (int32_t)(nchunks * (tc ? 4 : 2));
+    int status = 0;
+    for (int64_t k = 0; k < nchunks; ++k) {
+        const int64_t nc = (int64_t)hc_k[4 * k];
+        if (tc) total.candidates += nc;
+        if (tc && nc > ctx->cand_cap) *cand_overflow = std::max(*cand_overflow, nc);
+        status |= (int)(hc_k[4 * k + 2] & 0xffffffffu);
+    }
+    cudaEventElapsedTime(&total.kernel_ms, ctx->ev[1], ctx->ev[2]);
+    const int64_t nh_total = (int64_t)hc_k[4 * (nchunks - 1) + 1];
+    total.hits = nh_total;
+    ctx->stats = total;
+    *n_hits = nh_total;
+    if (status) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
+    if (*cand_overflow) return BLAMM_ERR_OVERFLOW;
+    return nh_total > hit_cap
+               ? fail(ctx, BLAMM_ERR_OVERFLOW, "%lld hits > capacity %lld", (long long)nh_total, (long long)hit_cap)
+               : BLAMM_OK;
+}
+
 // Whatever way the steps end, the chunk filter is reset and no copy into the caller's
-// buffers is still in flight.
+// buffers is still in flight.  A chunk whose candidates overflowed the buffer sends the
+// call to the synchronous chunked path, which grows the buffer and rescans.
 static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
                                int64_t nruns, blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
 {
-    const int rc = scan_host_pipelined_steps(ctx, bases, n, run_start, nruns, hits, hit_cap, n_hits);
+    int64_t cand_overflow = 0;
+    int rc = scan_host_async_steps(ctx, bases, n, run_start, nruns, hits, hit_cap, n_hits, &cand_overflow);
     ctx->keep_below = ctx->pos_base = 0;
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamSynchronize(ctx->stream);
+    if (rc == BLAMM_ERR_OVERFLOW && cand_overflow > 0) {
+        rc = scan_host_pipelined_steps(ctx, bases, n, run_start, nruns, hits, hit_cap, n_hits);
+        ctx->keep_below = ctx->pos_base = 0;
+        if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    }
     return rc;
 }
 
