@@ -225,3 +225,30 @@ def test_role_timing_instance_keeps_the_hit_set(scanner, mode):
     jobs = st["tiles"] * ((len(bases) + 127) // 128)
     assert 0 < prof.shape[0] <= jobs and int(prof[:, 10].sum()) == jobs
     assert (prof[:, 3] > 0).all()  # the issuers' loop time
+
+
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+def test_pipelined_scan_with_a_candidate_overflow_falls_back(mode):
+    """A permissive bank (3 % of positions x columns are hits) overflows the pipelined path's
+    candidate buffer in every chunk: the call falls back to the synchronous chunked path (its
+    per-chunk scan timing shows it) and still returns the device-resident scan's hits."""
+    torch = _torch()
+    from blamm_gb300 import GpuScanner
+    P, lens, thr = make_bank(93, 4, 5, 8, rel=0.85)
+    n = 34_000_000
+    bases, runs = make_stream(94, n, nruns=9)
+    sc = GpuScanner(0, mode)
+    try:
+        sc.set_motifs(P, lens, thr)
+        got = sc.scan(bases, runs)
+        assert sc.stats()["scan_ms"] > 0  # only the synchronous chunked path times its scans
+        d_b = torch.from_numpy(bases).cuda()
+        d_r = torch.from_numpy(runs).cuda()
+        cap = len(got) + 4096
+        d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+        assert len(got) > 5_000_000
+        ok, msg = same_hits(got, _hits(d_h, nh))
+        assert ok, msg
+    finally:
+        sc.close()
