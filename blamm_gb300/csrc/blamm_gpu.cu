@@ -759,13 +759,15 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     return BLAMM_OK;
 }
 
-static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
-                     int64_t hit_cap, int *launches)
+// The plain FP32 scan of n positions of the packed stream (seq2/zmask) on the context's
+// stream: parameters of the current bank and columns, hits appended through hit_count.
+static PlainParams plain_params(const blamm_ctx *ctx, const uint32_t *seq2, const uint32_t *zmask, int64_t n,
+                                const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits, int64_t hit_cap,
+                                unsigned long long *hit_count)
 {
-    CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     PlainParams p{};
-    p.seq2 = ctx->d_seq2;
-    p.zmask = ctx->d_zmask;
+    p.seq2 = seq2;
+    p.zmask = zmask;
     p.n = n;
     p.run_start = d_runs;
     p.nruns = nruns;
@@ -777,26 +779,44 @@ static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t n
     p.thr = ctx->d_thr;
     p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
     p.hits = d_hits;
-    p.hit_count = ctx->d_counters + 1;
+    p.hit_count = hit_count;
     p.hit_cap = hit_cap;
     p.keep_below = ctx->keep_below;
     p.pos_base = ctx->pos_base;
+    return p;
+}
+
+// Launch it: a block's columns staged in shared memory (as many as fit, at most 32).
+static int launch_plain(blamm_ctx *ctx, PlainParams &p)
+{
     const int threads = 256;
     int cpb = 32;
     while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
     p.cols_per_block = cpb;
     const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
-    const int64_t bx = (n + threads - 1) / threads;
+    const int64_t bx = (p.n + threads - 1) / threads;
     const int by = (p.ncols + cpb - 1) / cpb;
     if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
     if (bx > 0) {
-        CK(cudaEventRecord(ctx->ev[4], ctx->stream));
         scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
         CK(cudaGetLastError());
-        CK(cudaEventRecord(ctx->ev[5], ctx->stream));
-        ctx->plain_timed = true;
-        ++*launches;
     }
+    return BLAMM_OK;
+}
+
+static int run_plain(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
+                     int64_t hit_cap, int *launches)
+{
+    CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    PlainParams p = plain_params(ctx, ctx->d_seq2, ctx->d_zmask, n, d_runs, nruns, d_hits, hit_cap,
+                                 ctx->d_counters + 1);
+    if (n == 0) return BLAMM_OK;
+    CK(cudaEventRecord(ctx->ev[4], ctx->stream));
+    const int rc = launch_plain(ctx, p);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[5], ctx->stream));
+    ctx->plain_timed = true;
+    ++*launches;
     return BLAMM_OK;
 }
 
@@ -952,35 +972,8 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
                                                                           nwords32, ctx->lower_scores);
     CK(cudaGetLastError());
     if (ctx->mode == BLAMM_MODE_FP32) {
-        PlainParams p{};
-        p.seq2 = ctx->d_seq2;
-        p.zmask = ctx->d_zmask;
-        p.n = n;
-        p.run_start = d_runs;
-        p.nruns = nruns;
-        p.P = ctx->d_P;
-        p.p_rows = ctx->p_rows;
-        p.ncols = scanned_columns(ctx);
-        p.lmax = ctx->lmax;
-        p.col_len = ctx->d_len;
-        p.thr = ctx->d_thr;
-        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
-        p.hits = d_hits;
-        p.hit_count = cnt + 1;
-        p.hit_cap = hit_cap;
-        p.keep_below = ctx->keep_below;
-        p.pos_base = ctx->pos_base;
-        const int threads = 256;
-        int cpb = 32;
-        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
-        p.cols_per_block = cpb;
-        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
-        const int64_t bx = (n + threads - 1) / threads;
-        const int by = (p.ncols + cpb - 1) / cpb;
-        if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
-        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
-        CK(cudaGetLastError());
-        return BLAMM_OK;
+        PlainParams p = plain_params(ctx, ctx->d_seq2, ctx->d_zmask, n, d_runs, nruns, d_hits, hit_cap, cnt + 1);
+        return launch_plain(ctx, p);
     }
     launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
     CK(cudaGetLastError());
@@ -1562,32 +1555,8 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
     }
 
     if (!tc) {
-        PlainParams p{};
-        p.seq2 = seq2;
-        p.zmask = zmask;
-        p.n = n;
-        p.run_start = d_run_start;
-        p.nruns = nruns;
-        p.P = ctx->d_P;
-        p.p_rows = ctx->p_rows;
-        p.ncols = scanned_columns(ctx);
-        p.lmax = ctx->lmax;
-        p.col_len = ctx->d_len;
-        p.thr = ctx->d_thr;
-        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
-        p.hits = d_hits;
-        p.hit_count = counters + 1;
-        p.hit_cap = hit_cap;
-        const int threads = 256;
-        int cpb = 32;
-        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
-        p.cols_per_block = cpb;
-        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
-        const int64_t bx = (n + threads - 1) / threads;
-        const int by = (p.ncols + cpb - 1) / cpb;
-        if (by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
-        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
-        CK(cudaGetLastError());
+        PlainParams p = plain_params(ctx, seq2, zmask, n, d_run_start, nruns, d_hits, hit_cap, counters + 1);
+        if ((rc = launch_plain(ctx, p))) return rc;
         ++launches;
     } else {
         const int64_t n_mtiles = (n + kBM - 1) / kBM;
@@ -1714,33 +1683,8 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
         CK(cudaGetLastError());
     }
     if (!tc) {
-        PlainParams p{};
-        p.seq2 = ctx->d_seq2;
-        p.zmask = ctx->d_zmask;
-        p.n = n;
-        p.run_start = d_run_start;
-        p.nruns = nruns;
-        p.P = ctx->d_P;
-        p.p_rows = ctx->p_rows;
-        p.ncols = scanned_columns(ctx);
-        p.lmax = ctx->lmax;
-        p.col_len = ctx->d_len;
-        p.thr = ctx->d_thr;
-        p.cols = ctx->active.empty() ? nullptr : ctx->d_active;
-        p.hits = d_hits;
-        p.hit_count = cnt + 1;
-        p.hit_cap = hit_cap;
-        const int threads = 256;
-        int cpb = 32;
-        while (cpb > 1 && (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64 > (size_t)ctx->max_smem) cpb /= 2;
-        p.cols_per_block = cpb;
-        const size_t smem = (size_t)cpb * (p.p_rows + 2) * 4 + threads + p.lmax + 64;
-        const int64_t bx = (n + threads - 1) / threads;
-        const int by = (p.ncols + cpb - 1) / cpb;
-        if (bx > 0x7fffffff || by > 65535) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "grid too large");
-        scan_plain_kernel<<<dim3((unsigned)bx, (unsigned)by), threads, smem, ctx->stream>>>(p);
-        CK(cudaGetLastError());
-        return BLAMM_OK;
+        PlainParams p = plain_params(ctx, ctx->d_seq2, ctx->d_zmask, n, d_run_start, nruns, d_hits, hit_cap, cnt + 1);
+        return launch_plain(ctx, p);
     }
     const int64_t n_mtiles = (n + kBM - 1) / kBM;
     const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
