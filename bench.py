@@ -52,9 +52,9 @@ def args_parse():
                          "term count with the default tile plan (no autotuner launches, for profiling)")
     ap.add_argument("--serve-requests", type=int, default=48, help="distinct requests of the serving pool")
     ap.add_argument("--serve-slots", type=int, default=8, help="requests in flight in the serving measurement")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4"],
-                    help="config2 is the headline line; config3 (1 Gbp x 2000 motifs, precision at scale) and "
-                         "config4 (10,000 short sequences, batching) print their own measurement line")
+    ap.add_argument("--workload", default="genome_100mbp", choices=["genome_100mbp", "genome_1gbp", "promoters_10k"],
+                    help="genome_100mbp is the headline line; genome_1gbp (1 Gbp x 2000 motifs, precision at scale) and "
+                         "promoters_10k (10,000 short sequences, batching) print their own measurement line")
     return ap.parse_args()
 
 
@@ -69,7 +69,7 @@ def dist_env():
 def build_workload(seed: int, total: int):
     from blamm_gb300 import workloads
     from blamm_gb300._native import MotifBank
-    wl = workloads.config2(seed, total=total)
+    wl = workloads.genome_100mbp(seed, total=total)
     bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
     counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
     bank = MotifBank.from_pfms([p for _, p in wl.motifs], revcompl=True)
@@ -205,7 +205,7 @@ def run_reference(a, rank, world):
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic",
-        "config": {"workload": f"config2: 512 motifs (1024 columns, L 5-30, both strands) x "
+        "config": {"workload": f"genome_100mbp: 512 motifs (1024 columns, L 5-30, both strands) x "
                                f"{len(bases)} bp, p=1e-4; each step a {sample} bp sample"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"first {sample} bp of the stream x 1024 columns, "
@@ -253,24 +253,24 @@ def emitted_score_error(hits, ref, npos: int) -> dict:
             "note": "the reference's own FP32 sum; error = FP32 rounding of the sequential sum"}
 
 
-# ------------------------------------------------------------------ serving (config 5)
+# ------------------------------------------------------------------ serving
 def run_serve(a) -> dict:
-    """Config-5 serving through the scan service (include/blamm_serve.h): a resident bank of
+    """Serving through the scan service (include/blamm_serve.h): a resident bank of
     2000 motifs (4000 columns) with threshold sets for p = 1e-3, 1e-4, 1e-5; requests of
     log-uniform 1 kbp-5 Mbp, U{1..2000} motifs, a random p.  First the saturation throughput
     (every request queued at once), then Poisson arrivals at 25 / 50 / 90 % of it; latency =
     submission to completion, measured by the service."""
     from blamm_gb300 import Server, workloads
     from blamm_gb300._native import MotifBank
-    pfms = workloads.config5_bank(a.seed)
+    pfms = workloads.service_bank(a.seed)
     bank = MotifBank.from_pfms([p for _, p in pfms], revcompl=True)
     counts = np.array([2625, 2375, 2375, 2625], dtype=np.uint64)  # GC 0.475, the middle of the requests' range
     bank.generate(counts, 0.25)
     P, lens, _ = bank.matrix()
     bgp = ((counts.astype(np.float32) + np.float32(0.25)) /
            (np.float32(counts.sum()) + np.float32(1.0))).astype(np.float32)
-    sets = np.stack([bank.pvalue_thresholds(bgp, pv) for pv in workloads.CONFIG5_PVALUES])
-    reqs = workloads.config5_requests(a.seed, a.serve_requests)
+    sets = np.stack([bank.pvalue_thresholds(bgp, pv) for pv in workloads.SERVICE_PVALUES])
+    reqs = workloads.service_requests(a.seed, a.serve_requests)
     req_cols = [np.stack([2 * m, 2 * m + 1], axis=1).ravel().astype(np.int32) for _, _, m, _ in reqs]
     work = [len(b) * len(c) for (b, _, _, _), c in zip(reqs, req_cols)]
     srv = Server(P, lens, sets, slots=a.serve_slots)
@@ -285,7 +285,7 @@ def run_serve(a) -> dict:
         for i in ids:
             srv.take(i)
         sat_rate = len(reqs) / wall
-        out = {"workload": "config5: 2000 motifs (4000 columns), requests log-uniform 1 kbp-5 Mbp, "
+        out = {"workload": "service: 2000 motifs (4000 columns), requests log-uniform 1 kbp-5 Mbp, "
                            "U{1..2000} motifs, p in {1e-3, 1e-4, 1e-5}",
                "slots": a.serve_slots, "pool": len(reqs),
                "saturation": {"requests_per_s": sat_rate, "bp_motif_per_s": sum(work) / wall,
@@ -347,14 +347,14 @@ def _device_scan(sc, torch, d_b, n, d_r, nr, cap):
     return nh, d_h
 
 
-def run_config3(a):
-    """Config 3: 2000 motifs (4000 columns) over 1 Gbp (2nd-order Markov, GC 0.41, 1 % N runs),
+def run_genome_1gbp(a):
+    """2000 motifs (4000 columns) over 1 Gbp (2nd-order Markov, GC 0.41, 1 % N runs),
     p = 1e-4 and 1e-5 thresholds inverted in FP64 on the GPU; BF16 split vs single-term BF16
     (same hits required); the plain FP32 form on a 100 Mbp sample."""
     import torch
     from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
     t0 = time.perf_counter()
-    wl = workloads.config3(a.seed, total=a.bases if a.bases != 100_000_000 else 1_000_000_000)
+    wl = workloads.genome_1gbp(a.seed, total=a.bases if a.bases != 100_000_000 else 1_000_000_000)
     bases, runs, _, _ = workloads.filtered_stream(wl.sequences)
     gen_s = time.perf_counter() - t0
     counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
@@ -363,7 +363,7 @@ def run_config3(a):
     n, ncols = len(bases), P.shape[0]
     d_b = torch.from_numpy(bases).cuda()
     d_r = torch.from_numpy(runs).cuda()
-    out = {"workload": f"config3: 2000 motifs (4000 columns) x {n} bp (2nd-order Markov, GC 0.41, 1% N runs), "
+    out = {"workload": f"genome_1gbp: 2000 motifs (4000 columns) x {n} bp (2nd-order Markov, GC 0.41, 1% N runs), "
                        "thresholds from GPU theoretical histograms (FP64 inversion)",
            "generate_s": gen_s, "thresholds": tinfo, "runs": []}
     for pi, pv in enumerate((1e-4, 1e-5)):
@@ -415,14 +415,14 @@ def run_config3(a):
     print(json.dumps({"metric": METRIC, "config": out}), flush=True)
 
 
-def run_config4(a):
-    """Config 4: 10,000 promoter-like sequences (log-normal lengths, median 2 kbp, sigma 1.0,
+def run_promoters_10k(a):
+    """10,000 promoter-like sequences (log-normal lengths, median 2 kbp, sigma 1.0,
     clipped 200 bp-50 kbp, GC 0.5) x 800 motifs (1600 columns), p = 1e-4: one persistent launch
     over all sequences, the same as a CUDA graph, and one launch per sequence, in the default mode
     (one BF16 term until tuned); then the autotuned term count and plan."""
     import torch
     from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
-    wl = workloads.config4(a.seed)
+    wl = workloads.promoters_10k(a.seed)
     bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
     counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
     sc = GpuScanner(0, "auto")
@@ -475,7 +475,7 @@ def run_config4(a):
     tuned = timed(lambda: sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap))
     nh2 = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
     same = hit_digest(d_h[: nh2 * HIT_DTYPE.itemsize].cpu().numpy().view(HIT_DTYPE)) == batch
-    out = {"workload": f"config4: {len(wl.sequences)} sequences ({n} bp) x 800 motifs (1600 columns), p=1e-4",
+    out = {"workload": f"promoters_10k: {len(wl.sequences)} sequences ({n} bp) x 800 motifs (1600 columns), p=1e-4",
            "one_launch_ms": one, "one_launch_bp_motif_per_s": units / (one / 1e3),
            "graph_ms": graph_ms, "graph_bp_motif_per_s": units / (graph_ms / 1e3),
            "per_sequence_launches_ms": per_seq_ms, "per_sequence_bp_motif_per_s": units / (per_seq_ms / 1e3),
@@ -637,8 +637,8 @@ def run_ours(a, rank, world, local):
         "dtype": ("bf16x2 (hi+lo fixed-point split" if terms == 2 else "bf16 (one fixed-point term")
                  + ", fp32 accumulate) + fp32 rescoring"
                  + ("; term count autotuned" if a.mode == "auto" else ""),
-        "data": "synthetic (seeded numpy, config2 shapes)",
-        "config": {"workload": "config2: 512 motifs (1024 columns, L 5-30, both strands, Dirichlet(0.5) "
+        "data": "synthetic (seeded numpy; the 100 Mbp x 512-motif shapes)",
+        "config": {"workload": "genome_100mbp: 512 motifs (1024 columns, L 5-30, both strands, Dirichlet(0.5) "
                                "columns of 100 counts) x 24 iid sequences (A=T=0.29) log-uniform 1-20 Mbp, "
                                f"{n} bp per rank, p=1e-4 theoretical-histogram thresholds",
                    "bases_per_rank": n, "columns": ncols, "l2": "flushed (256 MiB write between steps)",
@@ -688,13 +688,13 @@ def main():
     if a.impl == "reference":
         run_reference(a, rank, world)
         return
-    if a.workload == "config3":
+    if a.workload == "genome_1gbp":
         if rank == 0:
-            run_config3(a)
+            run_genome_1gbp(a)
         return
-    if a.workload == "config4":
+    if a.workload == "promoters_10k":
         if rank == 0:
-            run_config4(a)
+            run_promoters_10k(a)
         return
     run_ours(a, rank, world, local)
 

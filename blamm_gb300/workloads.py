@@ -1,16 +1,16 @@
-"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+"""Seeded synthetic workloads with the shapes of the benchmark cases.
 
 The reference ships no benchmark data; these generators stand in for it:
-  config 1  32 motifs (L 6-20), 2 x 500 kbp iid (A=T=0.3, C=G=0.2)
-  config 2  512 motifs (L 5-30), 24 sequences log-uniform 1-20 Mbp, ~100 Mbp total
-            iid (A=T=0.29, C=G=0.21)
-  config 3  2000 motifs (L 5-30), 1 Gbp, 2nd-order Markov background (GC ~ 0.41),
-            1 % of bases in N runs of length log-uniform 100-10k
-  config 4  10,000 sequences, log-normal lengths (median 2 kbp, sigma 1.0,
-            clipped 200-50k), GC 0.5, 800 motifs (L 6-25)
-  config 5  serving: a resident bank of 2000 motifs (L 5-30); requests of log-uniform
-            length 1 kbp-5 Mbp (iid, GC ~ U[0.35, 0.6]), a subset of U{1..2000}
-            motifs and p in {1e-3, 1e-4, 1e-5}
+  two_sequences_1mbp  32 motifs (L 6-20), 2 x 500 kbp iid (A=T=0.3, C=G=0.2)
+  genome_100mbp       512 motifs (L 5-30), 24 sequences log-uniform 1-20 Mbp, ~100 Mbp
+                      total, iid (A=T=0.29, C=G=0.21)
+  genome_1gbp         2000 motifs (L 5-30), 1 Gbp, 2nd-order Markov background
+                      (GC ~ 0.41), 1 % of bases in N runs of length log-uniform 100-10k
+  promoters_10k       10,000 sequences, log-normal lengths (median 2 kbp, sigma 1.0,
+                      clipped 200-50k), GC 0.5, 800 motifs (L 6-25)
+  service_*           a resident bank of 2000 motifs (L 5-30); requests of log-uniform
+                      length 1 kbp-5 Mbp (iid, GC ~ U[0.35, 0.6]), a subset of
+                      U{1..2000} motifs and p in {1e-3, 1e-4, 1e-5}
 Motif columns are Multinomial(100, Dirichlet(0.5 * 1_4)) counts.  Random
 streams: numpy default_rng with separate children for motifs, lengths, bases.
 """
@@ -107,23 +107,23 @@ class Workload:
         return int(sum(len(s) for _, s in self.sequences))
 
 
-def config1(seed: int = 0, seq_len: int = 500_000) -> Workload:
+def two_sequences_1mbp(seed: int = 0, seq_len: int = 500_000) -> Workload:
     rm, rl, rb = rngs(seed)
     motifs = random_pfms(rm, 32, 6, 20)
     seqs = [(f"seq{i}", iid_bases(rb, seq_len, [0.3, 0.2, 0.2, 0.3])) for i in range(2)]
-    return Workload("config1", seqs, motifs, 1e-4)
+    return Workload("two_sequences_1mbp", seqs, motifs, 1e-4)
 
 
-def config2(seed: int = 0, total: int = 100_000_000, nseq: int = 24) -> Workload:
+def genome_100mbp(seed: int = 0, total: int = 100_000_000, nseq: int = 24) -> Workload:
     rm, rl, rb = rngs(seed)
     motifs = random_pfms(rm, 512, 5, 30)
     raw = np.exp(rl.uniform(np.log(1e6), np.log(2e7), size=nseq))
     lens = np.maximum(1, np.round(raw / raw.sum() * total)).astype(np.int64)
     seqs = [(f"chr{i + 1}", iid_bases(rb, int(L), [0.29, 0.21, 0.21, 0.29])) for i, L in enumerate(lens)]
-    return Workload("config2", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+    return Workload("genome_100mbp", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
 
 
-def config3(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Workload:
+def genome_1gbp(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Workload:
     rm, rl, rb = rngs(seed)
     motifs = random_pfms(rm, 2000, 5, 30)
     raw = np.exp(rl.uniform(np.log(1e6), np.log(2e7), size=nseq))
@@ -132,26 +132,26 @@ def config3(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Worklo
     for i, L in enumerate(lens):
         s = markov2_bases(rb, int(L), 0.41)
         seqs.append((f"chr{i + 1}", insert_n_runs(rb, s, 0.01)))
-    return Workload("config3", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+    return Workload("genome_1gbp", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
 
 
-def config4(seed: int = 0, nseq: int = 10_000) -> Workload:
+def promoters_10k(seed: int = 0, nseq: int = 10_000) -> Workload:
     rm, rl, rb = rngs(seed)
     motifs = random_pfms(rm, 800, 6, 25)
     lens = np.clip(np.round(np.exp(rl.normal(np.log(2000), 1.0, size=nseq))), 200, 50_000).astype(np.int64)
     seqs = [(f"prom{i}", iid_bases(rb, int(L), [0.25, 0.25, 0.25, 0.25])) for i, L in enumerate(lens)]
-    return Workload("config4", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+    return Workload("promoters_10k", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
 
 
-def config5_bank(seed: int = 0) -> list[tuple[str, np.ndarray]]:
+def service_bank(seed: int = 0) -> list[tuple[str, np.ndarray]]:
     rm, _, _ = rngs(seed)
     return random_pfms(rm, 2000, 5, 30)
 
 
-CONFIG5_PVALUES = (1e-3, 1e-4, 1e-5)
+SERVICE_PVALUES = (1e-3, 1e-4, 1e-5)
 
 
-def config5_requests(seed: int, k: int, nmotifs: int = 2000, max_len: int = 5_000_000):
+def service_requests(seed: int, k: int, nmotifs: int = 2000, max_len: int = 5_000_000):
     """k serving requests: (bases, run starts [0], motif indices (sorted), p-value index)."""
     rng = np.random.default_rng([seed, 5])
     out = []
@@ -161,7 +161,7 @@ def config5_requests(seed: int, k: int, nmotifs: int = 2000, max_len: int = 5_00
         b = iid_bases(rng, n, [(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])
         m = int(rng.integers(1, nmotifs + 1))
         motifs = np.sort(rng.choice(nmotifs, size=m, replace=False))
-        out.append((b, np.zeros(1, dtype=np.int64), motifs, int(rng.integers(0, len(CONFIG5_PVALUES)))))
+        out.append((b, np.zeros(1, dtype=np.int64), motifs, int(rng.integers(0, len(SERVICE_PVALUES)))))
     return out
 
 

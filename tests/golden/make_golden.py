@@ -108,9 +108,9 @@ def case_cb(d):
             "outputs": ["occ_pt.txt", "occ_rt.txt"]}
 
 
-def case_config1(d):
-    """Config 1 shapes at reduced size: 32 motifs (L 6-20), 2 x 100 kbp iid (A=T=0.3), -rc -pt 1e-4."""
-    wl = workloads.config1(0, seq_len=100_000)
+def case_two_sequences_1mbp(d):
+    """The two-sequence shapes at reduced size: 32 motifs (L 6-20), 2 x 100 kbp iid (A=T=0.3), -rc -pt 1e-4."""
+    wl = workloads.two_sequences_1mbp(0, seq_len=100_000)
     os.makedirs(os.path.join(d, "seqs"), exist_ok=True)
     workloads.write_fasta(os.path.join(d, "seqs", "seqs.fa"), wl.sequences)
     with open(os.path.join(d, "sequences.mf"), "w") as f:
@@ -125,7 +125,7 @@ def case_config1(d):
             "outputs": ["occ_pt.txt"]}
 
 
-CASES = {"mixed": case_mixed, "cb": case_cb, "config1": case_config1}
+CASES = {"mixed": case_mixed, "cb": case_cb, "two_sequences_1mbp": case_two_sequences_1mbp}
 
 
 def run_reference(d, spec):

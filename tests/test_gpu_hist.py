@@ -1,7 +1,7 @@
 """GPU theoretical histograms and p-value thresholds (blamm_theoretical_hist).
 
 Pinned two ways: the counts equal the reference's own hist_*.dat files of the
-config-1 golden case, and, on random banks, the oracle's restatement of the
+two-sequence golden case, and, on random banks, the oracle's restatement of the
 DP; the thresholds equal the host library's (whose CLI output matches the
 reference's files) bit for bit.  The FP64 DP variant is checked for closeness.
 """
@@ -16,7 +16,7 @@ from blamm_gb300._native import MotifBank
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "config1")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "two_sequences_1mbp")
 
 
 def _bg_prob(counts, pseudo=0.25):

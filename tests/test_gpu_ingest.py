@@ -84,9 +84,9 @@ def test_sequence_before_header_is_rejected(scanner):
 
 
 def test_nucleotide_counts_equal_the_reference_dictionary(scanner):
-    """The config-1 case's sequences.mf.dict (written by the reference's dict module) holds
+    """The two-sequence case's sequences.mf.dict (written by the reference's dict module) holds
     NUCL_COUNT_ACGT of its FASTA file; the GPU ingest gives the same four counts."""
-    d = os.path.join(GOLDEN, "config1")
+    d = os.path.join(GOLDEN, "two_sequences_1mbp")
     words = open(os.path.join(d, "expected", "sequences.mf.dict")).read().split()
     want = [int(x) for x in words[words.index("NUCL_COUNT_ACGT") + 1:][:4]]
     got = _gpu_parse(scanner, _concat([os.path.join(d, "seqs", "seqs.fa")]))
