@@ -192,3 +192,23 @@ def test_score_text_equals_printf_g():
         want = oracle.format_scores(v)
         bad = [i for i, (g, w) in enumerate(zip(got, want)) if g != w]
         assert not bad, [(float(v[i]), got[i], want[i]) for i in bad[:5]]
+
+
+def test_bench_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference (the reference's CPU algorithm, oracle port) prints one JSON
+    line with the keys the benchmark contract names, on a small workload."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--bases",
+                          "2000000", "--cpu-sample", "50000", "--steps", "1", "--warmup", "3"],
+                         cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
