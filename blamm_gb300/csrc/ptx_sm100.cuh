@@ -142,27 +142,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
     return d;
 }
 
-// Named barrier over `count` threads (a multiple of 32).
-__device__ __forceinline__ void bar_sync(int id, int count)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
-// Named barrier over `count` threads that also returns whether any of them
-// passed pred = true.
-__device__ __forceinline__ bool bar_any(int id, int count, bool pred)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, %2, %3, p;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)pred), "r"(id), "r"(count)
-        : "memory");
-    return r != 0;
-}
 
 // Instruction descriptor for kind::f16 with BF16 A and B, FP32 accumulate,
 // both operands K-major, dense: D format bits 4-5 = 1 (F32), A format bits
@@ -194,24 +173,9 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
 }
 
 // 32 lanes x 32 consecutive 32-bit columns: thread t of the warp receives the
-// 32 columns of TMEM lane (lane base of the address) + t.
-__device__ __forceinline__ void tmem_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[32])
-{
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-}
-
-// The same load, and the maximum of the thread's 32 values (as f32) in red:
-// the reduction comes with the load (sm_103a), no instructions on the registers.
+// 32 columns of TMEM lane (lane base of the address) + t, and the maximum of
+// its 32 values (as f32) in red: the reduction comes with the load (sm_103a),
+// no instructions on the registers.
 __device__ __forceinline__ void tmem_ld_max_32x32b_x32(uint32_t taddr, uint32_t (&r)[32], float &red)
 {
     asm volatile(
