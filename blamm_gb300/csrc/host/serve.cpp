@@ -123,7 +123,8 @@ void run_request(blamm_server *s, Slot &slot, Request &r)
     } else {
         r.hits.clear();
     }
-    if (rc != BLAMM_OK) {
+    if (rc != BLAMM_OK) {  // a failed request carries no hits
+        std::vector<blamm_hit>().swap(r.hits);
         r.status = rc;
         r.err = blamm_last_error(ctx);
     }

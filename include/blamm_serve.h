@@ -16,7 +16,10 @@
  *   - admission by device memory: a request is admitted when the device bytes
  *     it needs (stream, packed stream, candidates, hits, tile plan; an estimate
  *     made at submission) fit in what the requests in flight leave of the
- *     budget.  Admission is first in, first out;
+ *     budget.  Admission is first in, first out.  A slot's context keeps the
+ *     device buffers of the largest request it has run (they are reused, not
+ *     freed), and the budget counts requests in flight only: with requests
+ *     near the budget, set hbm_budget to the free memory divided by the slots;
  *   - results: the hits of a request are the same alone and in any mix (each
  *     request has its own context; scores are exact FP32, see blamm_gpu.h).
  *
