@@ -19,9 +19,11 @@
 // 1.0 in K slots 0-2 times three BF16 pieces of T), where T is the column's
 // threshold minus its guard band, rounded down to the grid u = 2^-(k+8).
 // Every partial sum is then an integer multiple of u below 2^24 u in
-// magnitude (motifs up to 256 long), i.e. exactly representable in FP32: the
-// accumulator holds sum(q) - T exactly, whatever the tensor cores' internal
-// rounding, and a position is a candidate iff its sign bit is clear.  The
+// magnitude (motifs up to 256 long), i.e. exactly representable in FP32, so an
+// accumulation that keeps 24 significant bits holds sum(q) - T exactly (the
+// raw-score dump instance compares the accumulator with the exact sum on
+// every position and column of a test bank), and a position is a candidate
+// iff its sign bit is clear.  The
 // guard band bounds |sum(q) - sum(P)| plus the reference's own FP32 rounding
 // of sum(P), so every reference hit is a candidate; candidates are rescored
 // in exact FP32 (rescore_kernel).
