@@ -1,36 +1,38 @@
-"""Splitting a filtered base stream over GPUs (one process per GPU).
+"""Splitting one filtered base stream over GPUs (one process per GPU).
 
-A window is scored only if it lies inside one run (the reference's
-run-length check, pwmscan.cpp:122-126), so cutting the stream at run starts
-gives shards that need no halo and no exchange: each rank scans its own
-shard, hit positions are shifted by the shard offset, and the union of the
-ranks' hits is the hit set of the whole stream.  The reference does the
-same with one host thread per device pulling blocks from a shared queue
-(pwmscan.cpp:439-453); with one process per GPU the split is static.
+Each rank takes a contiguous, equally long range [lo, hi) of window starts and scans
+bases[lo : hi + halo] with halo = longest motif - 1, so every window that starts in its
+range lies inside what it scans; hits starting at or after hi belong to the next rank and
+are dropped.  A window is scored only inside one run (the reference's run-length check,
+src/pwmscan.cpp:122-126), so the shard's run table is the run that holds lo, rebased to 0,
+and the runs that start after it.  No exchange is needed: the union of the ranks' hits,
+shifted by their offsets, is the hit set of the whole stream.  The reference does the same
+with overlapping blocks pulled from a shared queue by one host thread per device
+(src/sequence.cpp:274-293, src/pwmscan.cpp:439-453); with one process per GPU the split is
+static, and a stream that is one long run splits as evenly as any other.
 """
 from __future__ import annotations
 
 import numpy as np
 
 
-def shard_bounds(n: int, run_start: np.ndarray, world: int) -> list[tuple[int, int]]:
-    """world contiguous [lo, hi) ranges cut at run starts, balanced by bases."""
-    runs = np.asarray(run_start, dtype=np.int64)
-    cuts = [0]
-    for r in range(1, world):
-        target = n * r / world
-        i = int(np.argmin(np.abs(runs - target))) if len(runs) else 0
-        c = int(runs[i]) if len(runs) else 0
-        cuts.append(max(c, cuts[-1]))
-    cuts.append(n)
+def shard_bounds(n: int, world: int) -> list[tuple[int, int]]:
+    """world contiguous [lo, hi) ranges of window starts covering [0, n), lengths within 1."""
+    cuts = [n * r // world for r in range(world + 1)]
     return [(cuts[i], cuts[i + 1]) for i in range(world)]
 
 
-def shard(bases: np.ndarray, run_start: np.ndarray, rank: int, world: int):
-    """(bases, run_start, offset) of one rank's shard (run starts rebased)."""
-    lo, hi = shard_bounds(len(bases), run_start, world)[rank]
+def shard(bases: np.ndarray, run_start: np.ndarray, rank: int, world: int, halo: int):
+    """(bases, run_start, offset, keep) of one rank's shard.
+
+    The rank scans the returned bases with the returned run table, keeps the hits at
+    positions < keep and adds offset to their positions."""
+    if halo < 0:
+        raise ValueError("halo must be >= 0 (the longest motif - 1)")
+    n = len(bases)
+    lo, hi = shard_bounds(n, world)[rank]
+    end = min(n, hi + halo) if hi > lo else lo
     runs = np.asarray(run_start, dtype=np.int64)
-    sel = runs[(runs >= lo) & (runs < hi)] - lo
-    if hi > lo and (len(sel) == 0 or sel[0] != 0):
-        sel = np.concatenate([[0], sel])
-    return bases[lo:hi], sel.astype(np.int64), lo
+    inner = runs[(runs > lo) & (runs < end)] - lo
+    sel = np.concatenate([[0], inner]) if end > lo else inner
+    return bases[lo:end], sel.astype(np.int64), lo, hi - lo

@@ -114,13 +114,18 @@ def two_sequences_1mbp(seed: int = 0, seq_len: int = 500_000) -> Workload:
     return Workload("two_sequences_1mbp", seqs, motifs, 1e-4)
 
 
-def genome_100mbp(seed: int = 0, total: int = 100_000_000, nseq: int = 24) -> Workload:
+def genome_100mbp(seed: int = 0, total: int = 100_000_000, nseq: int = 24, part: int = 0) -> Workload:
+    """part > 0: another `total`-base part of a larger genome (its own sequence lengths and
+    bases, the same motifs); part 0 is the workload itself."""
     rm, rl, rb = rngs(seed)
+    if part > 0:
+        rl, rb = (np.random.default_rng(s) for s in np.random.SeedSequence([seed, part]).spawn(2))
     motifs = random_pfms(rm, 512, 5, 30)
     raw = np.exp(rl.uniform(np.log(1e6), np.log(2e7), size=nseq))
     lens = np.maximum(1, np.round(raw / raw.sum() * total)).astype(np.int64)
-    seqs = [(f"chr{i + 1}", iid_bases(rb, int(L), [0.29, 0.21, 0.21, 0.29])) for i, L in enumerate(lens)]
-    return Workload("genome_100mbp", seqs, motifs, 1e-4, {"lengths": lens.tolist()})
+    seqs = [(f"chr{part * nseq + i + 1}", iid_bases(rb, int(L), [0.29, 0.21, 0.21, 0.29]))
+            for i, L in enumerate(lens)]
+    return Workload("genome_100mbp", seqs, motifs, 1e-4, {"lengths": lens.tolist(), "part": part})
 
 
 def genome_1gbp(seed: int = 0, total: int = 1_000_000_000, nseq: int = 24) -> Workload:

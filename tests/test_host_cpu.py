@@ -125,6 +125,20 @@ def test_every_declared_symbol_is_exported():
             assert hasattr(lib, name), f"{header}: {name} is not exported"
 
 
+def test_genome_parts_share_the_bank_and_not_the_bases():
+    """The parts the benchmark's ranks scan at N > 1: one motif bank, distinct sequences;
+    part 0 is the single-GPU workload itself."""
+    a = workloads.genome_100mbp(0, total=300_000, nseq=4)
+    a0 = workloads.genome_100mbp(0, total=300_000, nseq=4, part=0)
+    b = workloads.genome_100mbp(0, total=300_000, nseq=4, part=1)
+    assert all(np.array_equal(x[1], y[1]) for x, y in zip(a.motifs, b.motifs))
+    assert all(np.array_equal(x[1], y[1]) for x, y in zip(a.sequences, a0.sequences))
+    assert [s for s, _ in a.sequences] == ["chr1", "chr2", "chr3", "chr4"]
+    assert [s for s, _ in b.sequences] == ["chr5", "chr6", "chr7", "chr8"]
+    assert abs(b.total_bases - 300_000) <= 4
+    assert not np.array_equal(a.sequences[0][1][:1000], b.sequences[0][1][:1000])
+
+
 REFERENCE_SRC = "/root/reference/src"
 CUDA_INCLUDE = "/usr/local/cuda/include"
 
