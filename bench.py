@@ -652,6 +652,8 @@ def run_ours(a, rank, world, local):
                    "bases_per_rank": n, "columns": ncols, "l2": "flushed (256 MiB write between steps)",
                    "parallelism": f"{world} rank(s), each its own {n} bp part of the genome, no collective",
                    "autotuned": tuned},
+        # the same rate counting a motif's forward and reverse-strand columns once
+        "value_per_distinct_motif": value * len(wl.motifs) / ncols,
         "hits": int(nh), "candidates": int(st["candidates"]), "tiles": int(st["tiles"]),
         "scan_kernel_ms": kern_ms, "rescore_kernel_ms": float(st["rescore_ms"]),
         "wall_s_timed_region": wall,
