@@ -166,14 +166,15 @@ def hit_digest(h: np.ndarray) -> tuple[int, int]:
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_sample_scan(bases, runs, P, lens, thr, sample: int):
-    """The reference's BLAS loop (oracle port) on the first `sample` bases, all cores."""
+def cpu_sample_scan(bases, runs, P, lens, thr, sample: int, threads: int | None = None):
+    """The reference's BLAS loop (oracle port) on the first `sample` bases, all cores
+    (or `threads` workers, the reference's -t)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     b = bases[:sample]
     r = runs[runs < len(b)]
     tiles = oracle.matrix_tiles(lens, 4096)
-    cores = os.cpu_count() or 1
+    cores = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     h = oracle.scan_blas(b, r, P, lens, thr, tiles, 1000, 250, cores)
     dt = time.perf_counter() - t0
@@ -685,6 +686,11 @@ def run_ours(a, rank, world, local):
                                 "sample": f"first {min(a.cpu_sample, n)} bp x {ncols} columns in {dt:.1f} s: the "
                                           "reference's BLAS block loop (h=1000, w=250, OpenBLAS sgemm per tile "
                                           "per offset, one BLAS thread per worker)"}
+        # the reference's -t 1 on a sixteenth of that sample (a few seconds of one core)
+        s1 = max(1, min(a.cpu_sample // 16, n))
+        v1, _, dt1, _ = cpu_sample_scan(bases, runs, P, lens, thr, s1, threads=1)
+        line["cpu_baseline"]["one_thread"] = {"value": v1, "unit": UNIT,
+                                              "sample": f"first {s1} bp x {ncols} columns in {dt1:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     sc.close()
