@@ -181,6 +181,26 @@ def cpu_sample_scan(bases, runs, P, lens, thr, sample: int, threads: int | None 
     return len(b) * P.shape[0] / dt, cores, dt, len(h)
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def run_reference(a, rank, world):
     """--impl reference: the reference's CPU scan (oracle port of its BLAS loop) per step."""
     if rank != 0:
@@ -203,7 +223,7 @@ def run_reference(a, rank, world):
         "data": "synthetic",
         "config": {"workload": f"genome_100mbp: 512 motifs (1024 columns, L 5-30, both strands) x "
                                f"{len(bases)} bp, p=1e-4; each step a {sample} bp sample"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                          "sample": f"first {sample} bp of the stream x 1024 columns, "
                                    "the reference's BLAS block loop (h=1000, w=250) on OpenBLAS"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -682,7 +702,7 @@ def run_ours(a, rank, world, local):
             line["serve_p99_ms"] = line["serve"]["open_loop"][-1]["p99_ms"]
     if rank == 0 and world == 1:
         v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                                 "sample": f"first {min(a.cpu_sample, n)} bp x {ncols} columns in {dt:.1f} s: the "
                                           "reference's BLAS block loop (h=1000, w=250, OpenBLAS sgemm per tile "
                                           "per offset, one BLAS thread per worker)"}
