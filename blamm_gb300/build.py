@@ -62,7 +62,7 @@ def _gpu_lib(force: bool) -> str:
     if force or _stale(out, deps):
         _run([_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-shared", "-o", out,
-              os.path.join(CSRC, "blamm_gpu.cu"), "-lcudart"])
+              os.path.join(CSRC, "blamm_gpu.cu"), "-lcudart", "-ldl"])  # -ldl: NVTX finds its tool by dlopen
     return out
 
 

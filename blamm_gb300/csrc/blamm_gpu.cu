@@ -23,6 +23,19 @@
 #include "hist_kernels.cuh"
 #include "ingest_kernels.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
+// A named range on the profiler timeline (nsys, ncu --nvtx) around each entry point;
+// NVTX calls do nothing unless a tool is attached.
+namespace {
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+}  // namespace
+
 using namespace blamm;
 
 static_assert(sizeof(blamm_hit) == sizeof(HitRec), "hit record layout");
@@ -490,6 +503,7 @@ int blamm_set_mode(blamm_ctx *ctx, int mode)
 int blamm_set_motifs(blamm_ctx *ctx, const float *P, int p_rows, int ncols, const int32_t *col_len,
                      const float *thr)
 {
+    const NvtxRange nvtx_range("blamm_set_motifs");
     if (!ctx) return BLAMM_ERR_ARG;
     if (!P || !col_len || !thr || ncols <= 0 || p_rows <= 0 || p_rows % 4)
         return fail(ctx, BLAMM_ERR_ARG, "invalid motif bank arguments");
@@ -859,6 +873,7 @@ extern "C" {
 int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
                       int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, int64_t *n_hits)
 {
+    const NvtxRange nvtx_range("blamm_scan_device");
     if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
     *n_hits = 0;
     if (n == 0) return BLAMM_OK;
@@ -1186,6 +1201,7 @@ static int scan_host_pipelined(blamm_ctx *ctx, const char *bases, int64_t n, con
 int blamm_scan(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start, int64_t nruns,
                blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
 {
+    const NvtxRange nvtx_range("blamm_scan");
     if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
     *n_hits = 0;
     if (n == 0) return BLAMM_OK;
@@ -1286,6 +1302,7 @@ int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const i
                            int64_t nruns, const float *min_score, const float *width, int nbins,
                            uint64_t *counts)
 {
+    const NvtxRange nvtx_range("blamm_score_histograms");
     if (!ctx || n < 0 || nbins <= 0 || !min_score || !width || !counts) return BLAMM_ERR_ARG;
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
     if (n == 0) return BLAMM_OK;
@@ -1510,6 +1527,7 @@ extern "C" {
 int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start,
                              int64_t nruns, blamm_hit *d_hits, int64_t hit_cap, int64_t *n_hits)
 {
+    const NvtxRange nvtx_range("blamm_scan_device_static");
     if (!ctx || !n_hits || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
     *n_hits = 0;
     if (n > kStaticMaxBases)
@@ -1633,6 +1651,7 @@ extern "C" {
 
 int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
 {
+    const NvtxRange nvtx_range("blamm_reserve");
     if (!ctx || max_positions < 0 || max_candidates < 0) return BLAMM_ERR_ARG;
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     CK(cudaSetDevice(ctx->device));
@@ -1657,6 +1676,7 @@ int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
 int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start, int64_t nruns,
                        blamm_hit *d_hits, int64_t hit_cap, uint64_t *d_counts)
 {
+    const NvtxRange nvtx_range("blamm_scan_enqueue");
     if (!ctx || !d_counts || n < 0 || hit_cap < 0) return BLAMM_ERR_ARG;
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     const int64_t nwords32 = (n + kStreamPad + 31) / 32;
@@ -1749,6 +1769,7 @@ int blamm_scan_graph_create(blamm_ctx *ctx, const char *d_bases, int64_t n, cons
 
 int blamm_scan_graph_launch(blamm_ctx *ctx, void *graph)
 {
+    const NvtxRange nvtx_range("blamm_scan_graph_launch");
     if (!ctx || !graph) return BLAMM_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
     CK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph), ctx->stream));
@@ -1786,6 +1807,7 @@ int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *j
 int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *d_run_start, int64_t nruns,
                    float *best_ms)
 {
+    const NvtxRange nvtx_range("blamm_autotune");
     if (!ctx || n < 0) return BLAMM_ERR_ARG;
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     if (best_ms) *best_ms = 0.0f;
@@ -1859,6 +1881,7 @@ int blamm_theoretical_hist(blamm_ctx *ctx, const float *P, int p_rows, int ncols
                            const int32_t *hist_of, const float bg_prob[4], int nbins, uint64_t max_length,
                            int fp64_dp, const float *pvalues, int npv, float *thr, uint64_t *counts)
 {
+    const NvtxRange nvtx_range("blamm_theoretical_hist");
     if (!ctx || !P || !col_len || !bg_prob || ncols <= 0 || p_rows <= 0 || nbins < 1 || nbins > 4096 ||
         npv < 0 || (npv > 0 && (!pvalues || !thr)))
         return BLAMM_ERR_ARG;
@@ -1967,6 +1990,7 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
                              int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
                              int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts)
 {
+    const NvtxRange nvtx_range("blamm_fasta_parse_device");
     if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs) return BLAMM_ERR_ARG;
     *n_bases = *nruns = *nseqs = 0;
     if (nucl_counts)
