@@ -134,7 +134,10 @@ int blamm_scan_device(blamm_ctx *ctx, const char *d_bases, int64_t n,
 /* Drop-in for the reference's kernel_wrapper (src/kernel.cu:36-45): for the
  * column-major m x n matrix d_R, append every entry R(i,j) >= d_threshold[j]
  * to d_occScore / d_occIdx (index j*m+i) at atomically reserved slots of
- * *d_nOcc.  Device pointers; runs on the context's stream and synchronises. */
+ * *d_nOcc.  Device pointers; runs on the context's stream and synchronises.
+ * Like kernel_wrapper it writes without a capacity check: one call appends at
+ * most m*n entries, so buffers of 2*m*n entries (the reference's, allocated at
+ * src/pwmscan.cpp:346-352) hold a call's output while *d_nOcc <= m*n. */
 int blamm_filter_score(blamm_ctx *ctx, float *d_R, int m, int n, const float *d_threshold,
                        int *d_occIdx, float *d_occScore, int *d_nOcc);
 
