@@ -51,6 +51,74 @@ def test_oracle_matches_reference_on_its_example(tmp_path):
     assert len(a) > 0
 
 
+def _random_case(d, seed: int) -> list[list[str]]:
+    """A small case of fresh inputs: two species groups, N runs, lowercase stretches, ragged
+    FASTA lines and blank lines, JASPAR or Cluster-Buster motifs, blocks of 20 kbp (the
+    reference's default block height h = 1000 with w = 20: at h = 100 this OpenBLAS build
+    rounds a few sgemm entries differently from motif-position order)."""
+    from blamm_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    motifs = workloads.random_pfms(rng, 10, 4, 22)
+    jaspar = seed % 2 == 0
+    mfile = "motifs.jaspar" if jaspar else "motifs.cb"
+    (workloads.write_jaspar if jaspar else workloads.write_cb)(str(d / mfile), motifs)
+    workloads.write_settings(str(d / "settings.cnf"), w=20, h=1000)
+    manifest = []
+    for g, nfiles in (("groupA", 2), ("groupB", 1)):
+        for f in range(nfiles):
+            name = f"{g}_{f}.fa"
+            with open(d / name, "wb") as out:
+                for s in range(int(rng.integers(1, 4))):
+                    seq = workloads.iid_bases(rng, int(rng.integers(2_000, 20_000)), [0.3, 0.2, 0.2, 0.3]).copy()
+                    for _ in range(int(rng.integers(0, 4))):  # N runs
+                        a = int(rng.integers(0, len(seq)))
+                        seq[a:a + int(rng.integers(1, 300))] = ord("N")
+                    for _ in range(int(rng.integers(0, 4))):  # lowercase (soft-masked) stretches
+                        a = int(rng.integers(0, len(seq)))
+                        seq[a:a + int(rng.integers(1, 500))] |= 0x20
+                    out.write(f">{g}_seq{f}_{s} description\n".encode())
+                    i = 0
+                    while i < len(seq):
+                        w = int(rng.integers(20, 100))
+                        out.write(seq[i:i + w].tobytes() + b"\n")
+                        if rng.random() < 0.02:
+                            out.write(b"\n")
+                        i += w
+            manifest.append(f"{g}\t{name}\n")
+    (d / "sequences.mf").write_text("".join(manifest))
+    return [["dict", "sequences.mf"],
+            ["hist", "-b", "120", mfile, "sequences.mf"],
+            ["scan", "-rc", "-pt", "0.001", "-o", "occ_pt.txt", mfile, "sequences.mf"],
+            ["scan", "-s", "-rt", "0.85", "-o", "occ_s.txt", mfile, "sequences.mf"],
+            ["scan", "-rc", "-at", "5", "-o", "occ_at.txt", mfile, "sequences.mf"]]
+
+
+@pytest.mark.skipif(not os.path.exists(oracle.REF_CLI_PATH), reason="reference binary only in the development container")
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_matches_reference_on_random_cases(tmp_path, seed):
+    """Differential check on fresh inputs: the compiled reference and the oracle write the
+    same dictionary, histograms, thresholds and occurrences."""
+    outs = {}
+    for name, binary in (("ref", oracle.REF_CLI_PATH), ("orc", oracle.CLI_PATH)):
+        d = tmp_path / name
+        d.mkdir()
+        cmds = _random_case(d, seed)
+        env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
+        for cmd in cmds:
+            subprocess.run([binary] + cmd, cwd=d, env=env, check=True, stdout=subprocess.DEVNULL)
+        outs[name] = d
+    ref, orc = outs["ref"], outs["orc"]
+    hists = sorted(p.name for p in ref.glob("hist_*"))
+    assert len(hists) == 40  # 10 motifs x 2 groups, a .dat and a .gnu file each
+    for f in ["sequences.mf.dict"] + hists:
+        assert (ref / f).read_bytes() == (orc / f).read_bytes(), f
+    for f in ("PWMthresholds.txt", "occ_pt.txt", "occ_s.txt", "occ_at.txt"):
+        a = sorted((ref / f).read_bytes().splitlines())
+        b = sorted((orc / f).read_bytes().splitlines())
+        assert a == b, f"{f}: {len(a)} vs {len(b)} lines"
+        assert len(a) > 0, f
+
+
 def test_blas_port_equals_sequential_scan():
     """OpenBLAS sums the one-hot products in motif-position order: the reference's
     BLAS loop and the sequential FP32 scorer agree bit for bit."""
