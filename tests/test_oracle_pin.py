@@ -93,30 +93,72 @@ def _random_case(d, seed: int) -> list[list[str]]:
             ["scan", "-rc", "-at", "5", "-o", "occ_at.txt", mfile, "sequences.mf"]]
 
 
-@pytest.mark.skipif(not os.path.exists(oracle.REF_CLI_PATH), reason="reference binary only in the development container")
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_oracle_matches_reference_on_random_cases(tmp_path, seed):
-    """Differential check on fresh inputs: the compiled reference and the oracle write the
+def _edge_case(d, crlf: bool) -> list[list[str]]:
+    """FASTA edge cases: a header without bases, a sequence shorter than every motif, IUPAC
+    codes and lowercase n inside a sequence, a soft-masked stretch, no newline at the end of
+    the file; LF or CRLF line ends."""
+    from blamm_gb300 import workloads
+    rng = np.random.default_rng(99)
+    workloads.write_jaspar(str(d / "m.jaspar"), workloads.random_pfms(rng, 8, 4, 16))
+    workloads.write_settings(str(d / "settings.cnf"), w=20, h=1000)
+    eol = b"\r\n" if crlf else b"\n"
+    seq = workloads.iid_bases(rng, 30_000, [0.3, 0.2, 0.2, 0.3]).copy()
+    iupac = np.frombuffer(b"RYKMSWBDHVNn", np.uint8)
+    for _ in range(40):
+        a = int(rng.integers(0, len(seq)))
+        seq[a:a + int(rng.integers(1, 5))] = iupac[int(rng.integers(0, len(iupac)))]
+    seq[1000:1500] |= 0x20
+    with open(d / "a.fa", "wb") as f:
+        f.write(b">empty" + eol + b">short" + eol + b"ACG" + eol + b">iupac x y" + eol)
+        for i in range(0, len(seq), 61):
+            f.write(seq[i:i + 61].tobytes() + eol)
+        f.write(b">last" + eol + workloads.iid_bases(rng, 500, [0.25] * 4).tobytes())
+    (d / "sequences.mf").write_text("g\ta.fa\n")
+    return [["dict", "sequences.mf"], ["hist", "-b", "80", "m.jaspar", "sequences.mf"],
+            ["scan", "-rc", "-pt", "0.01", "-o", "occ_pt.txt", "m.jaspar", "sequences.mf"],
+            ["scan", "-s", "-rc", "-rt", "0.8", "-o", "occ_s.txt", "m.jaspar", "sequences.mf"]]
+
+
+def _differential(tmp_path, make) -> None:
+    """Run the compiled reference and the oracle on the same fresh case; they must write the
     same dictionary, histograms, thresholds and occurrences."""
     outs = {}
     for name, binary in (("ref", oracle.REF_CLI_PATH), ("orc", oracle.CLI_PATH)):
         d = tmp_path / name
         d.mkdir()
-        cmds = _random_case(d, seed)
+        cmds = make(d)
         env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
         for cmd in cmds:
             subprocess.run([binary] + cmd, cwd=d, env=env, check=True, stdout=subprocess.DEVNULL)
         outs[name] = d
     ref, orc = outs["ref"], outs["orc"]
     hists = sorted(p.name for p in ref.glob("hist_*"))
-    assert len(hists) == 40  # 10 motifs x 2 groups, a .dat and a .gnu file each
+    assert len(hists) > 0
     for f in ["sequences.mf.dict"] + hists:
         assert (ref / f).read_bytes() == (orc / f).read_bytes(), f
-    for f in ("PWMthresholds.txt", "occ_pt.txt", "occ_s.txt", "occ_at.txt"):
+    occ = sorted(p.name for p in ref.glob("occ_*.txt"))
+    assert len(occ) == sum(c[0] == "scan" for c in cmds)
+    for f in ["PWMthresholds.txt"] + occ:
         a = sorted((ref / f).read_bytes().splitlines())
         b = sorted((orc / f).read_bytes().splitlines())
         assert a == b, f"{f}: {len(a)} vs {len(b)} lines"
         assert len(a) > 0, f
+
+
+NEEDS_REF = pytest.mark.skipif(not os.path.exists(oracle.REF_CLI_PATH),
+                               reason="reference binary only in the development container")
+
+
+@NEEDS_REF
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_matches_reference_on_random_cases(tmp_path, seed):
+    _differential(tmp_path, lambda d: _random_case(d, seed))
+
+
+@NEEDS_REF
+@pytest.mark.parametrize("crlf", [False, True])
+def test_oracle_matches_reference_on_fasta_edge_cases(tmp_path, crlf):
+    _differential(tmp_path, lambda d: _edge_case(d, crlf))
 
 
 def test_blas_port_equals_sequential_scan():
