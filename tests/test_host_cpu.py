@@ -93,6 +93,45 @@ def _oracle_stream(files, max_filt=-1):
 @pytest.mark.parametrize("max_filt", [-1, 30_001])
 def test_fasta_chunks_equal_oracle_stream(payload, overlap, max_filt):
     files = [os.path.join(gc.GOLDEN, "mixed", "seqs", f) for f in ("a_file.fa", "b_file.fa")]
+    _check_chunks(files, payload, overlap, max_filt)
+
+
+@pytest.mark.parametrize("crlf", [False, True])
+def test_fasta_edge_cases_stream_like_the_oracle(tmp_path, crlf):
+    """A header without bases, a 3-base sequence, IUPAC codes, no final newline, CRLF."""
+    from fresh_cases import edge_case
+    edge_case(tmp_path, crlf)
+    files = [str(tmp_path / "a.fa")]
+    for payload, overlap in ((10_000_000, 15), (997, 15), (64, 0)):
+        _check_chunks(files, payload, overlap, -1)
+    rd = FastaReader(files, -1)
+    while rd.next_chunk(1 << 20, 15) is not None:
+        pass
+    assert rd.sequence_names() == ["empty", "short", "iupac", "last"]
+
+
+@pytest.mark.skipif(not os.path.exists(oracle.REF_CLI_PATH), reason="reference binary only in the development container")
+@pytest.mark.parametrize("crlf", [False, True])
+def test_cli_dict_and_hist_match_reference_on_fasta_edge_cases(tmp_path, crlf):
+    import subprocess
+    from fresh_cases import edge_case
+    outs = {}
+    for name, binary in (("ref", oracle.REF_CLI_PATH), ("ours", CLI_PATH)):
+        d = tmp_path / name
+        d.mkdir()
+        cmds = [c for c in edge_case(d, crlf) if c[0] != "scan"]
+        for cmd in cmds:
+            subprocess.run([binary] + cmd, cwd=d, check=True, stdout=subprocess.DEVNULL,
+                           env=dict(os.environ, OPENBLAS_NUM_THREADS="1"))
+        outs[name] = d
+    files = ["sequences.mf.dict"] + sorted(p.name for p in outs["ref"].glob("hist_*"))
+    assert len(files) > 1
+    for f in files:
+        assert (outs["ref"] / f).read_bytes() == (outs["ours"] / f).read_bytes(), f
+
+
+def _check_chunks(files, payload, overlap, max_filt):
+    """The C++ reader's chunks against the oracle's stream of the same files."""
     bases, rs, rq, rp = _oracle_stream(files, max_filt)
     rd = FastaReader(files, max_filt)
     pos = 0
