@@ -111,15 +111,18 @@ def test_fasta_edge_cases_stream_like_the_oracle(tmp_path, crlf):
 
 
 @pytest.mark.skipif(not os.path.exists(oracle.REF_CLI_PATH), reason="reference binary only in the development container")
-@pytest.mark.parametrize("crlf", [False, True])
-def test_cli_dict_and_hist_match_reference_on_fasta_edge_cases(tmp_path, crlf):
+@pytest.mark.parametrize("kind,arg", [("edge", False), ("edge", True), ("random", 0), ("random", 1)])
+def test_cli_dict_and_hist_match_reference_on_fresh_cases(tmp_path, kind, arg):
+    """FASTA edge cases (LF, CRLF) and seeded random cases (two species groups, N runs,
+    soft-masked stretches, JASPAR and Cluster-Buster motifs)."""
     import subprocess
-    from fresh_cases import edge_case
+    from fresh_cases import edge_case, random_case
+    make = edge_case if kind == "edge" else random_case
     outs = {}
     for name, binary in (("ref", oracle.REF_CLI_PATH), ("ours", CLI_PATH)):
         d = tmp_path / name
         d.mkdir()
-        cmds = [c for c in edge_case(d, crlf) if c[0] != "scan"]
+        cmds = [c for c in make(d, arg) if c[0] != "scan"]
         for cmd in cmds:
             subprocess.run([binary] + cmd, cwd=d, check=True, stdout=subprocess.DEVNULL,
                            env=dict(os.environ, OPENBLAS_NUM_THREADS="1"))
