@@ -66,23 +66,53 @@ def dist_env():
 
 
 # ------------------------------------------------------------------ workload
-def build_workload(seed: int, total: int, part: int = 0, genome_counts=None):
-    """genome_100mbp (part 0) or another part of the same genome; genome_counts maps this
-    part's A/C/G/T counts to the whole genome's (the PWM background of every part)."""
-    from blamm_gb300 import workloads
-    from blamm_gb300._native import MotifBank
+def _genome(seed: int, total: int, part: int, genome_counts):
+    from blamm_gb300 import workloads  # numpy generators only: no native library is loaded
     wl = workloads.genome_100mbp(seed, total=total, part=part)
     bases, runs, rseq, _ = workloads.filtered_stream(wl.sequences)
     counts = np.array([np.count_nonzero((bases | 0x20) == ord(c)) for c in "acgt"], dtype=np.uint64)
     if genome_counts is not None:
         counts = genome_counts(counts)
+    return wl, bases, runs, rseq, counts
+
+
+def build_workload(seed: int, total: int, part: int = 0, genome_counts=None):
+    """genome_100mbp (part 0) or another part of the same genome through the product's host
+    library (motif bank, PWMs, p-value thresholds); genome_counts maps this part's A/C/G/T
+    counts to the whole genome's (the PWM background of every part).  Also returns, per P
+    column, the index of its PFM in the workload's motif list and its strand (1 = reverse)."""
+    from blamm_gb300._native import MotifBank
+    wl, bases, runs, rseq, counts = _genome(seed, total, part, genome_counts)
     bank = MotifBank.from_pfms([p for _, p in wl.motifs], revcompl=True)
     bank.generate(counts, 0.25)
-    P, lens, _ = bank.matrix()
+    P, lens, rc = bank.matrix()
     tot = np.float32(counts.sum()) + np.float32(4.0) * np.float32(0.25)
     bgp = ((counts.astype(np.float32) + np.float32(0.25)) / tot).astype(np.float32)
     thr = bank.pvalue_thresholds(bgp, wl.pvalue)
-    return wl, bases, runs, rseq, P, lens, thr
+    colmotif = np.array([int(bank.name(c)[1:]) for c in range(P.shape[0])], dtype=np.int64)
+    return wl, bases, runs, rseq, P, lens, thr, (colmotif, rc.astype(np.int8))
+
+
+def build_workload_oracle(seed: int, total: int):
+    """The same workload set up by the oracle alone (the reference's PWM, matrix and threshold
+    steps restated in C): the reference arm loads nothing of the product."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    wl, bases, runs, rseq, counts = _genome(seed, total, 0, None)
+    P, lens, thr, colmotif, strand = oracle.motif_bank([p for _, p in wl.motifs], counts, 0.25, (wl.pvalue,))
+    return wl, bases, runs, rseq, P, lens, thr[0], (colmotif, strand)
+
+
+def sample_digest(h: np.ndarray, colkey) -> dict:
+    """Order-independent digest of a hit set keyed by (position, PFM index, strand, score bits),
+    so that two differently ordered banks of the same motifs compare."""
+    colmotif, strand = colkey
+    if len(h) == 0:
+        return {"hits": 0, "digest": 0}
+    key = ((h["pos"].astype(np.uint64) << np.uint64(24)) ^ (colmotif[h["col"]].astype(np.uint64) << np.uint64(1))
+           ^ strand[h["col"]].astype(np.uint64)) * np.uint64(0x9E3779B97F4A7C15)
+    key ^= h["score"].view(np.uint32).astype(np.uint64) * np.uint64(0xC2B2AE3D27D4EB4F)
+    return {"hits": int(len(h)), "digest": int(np.bitwise_xor.reduce(key))}
 
 
 # ------------------------------------------------------------------ clocks
@@ -168,7 +198,8 @@ def hit_digest(h: np.ndarray) -> tuple[int, int]:
 # ------------------------------------------------------------------ CPU side
 def cpu_sample_scan(bases, runs, P, lens, thr, sample: int, threads: int | None = None):
     """The reference's BLAS loop (oracle port) on the first `sample` bases, all cores
-    (or `threads` workers, the reference's -t)."""
+    (or `threads` workers, the reference's -t).  Returns (rate, cores, seconds, hits): the
+    hits of every window that ends inside the sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     b = bases[:sample]
@@ -178,7 +209,84 @@ def cpu_sample_scan(bases, runs, P, lens, thr, sample: int, threads: int | None 
     t0 = time.perf_counter()
     h = oracle.scan_blas(b, r, P, lens, thr, tiles, 1000, 250, cores)
     dt = time.perf_counter() - t0
-    return len(b) * P.shape[0] / dt, cores, dt, len(h)
+    return len(b) * P.shape[0] / dt, cores, dt, h
+
+
+def restrict_to_sample(h: np.ndarray, lens, sample: int) -> np.ndarray:
+    """Hits of a whole-stream scan whose window ends inside the first `sample` bases."""
+    return h[h["pos"] + lens[h["col"]] <= sample]
+
+
+def parity_vs_oracle(gpu_hits: np.ndarray, oracle_hits: np.ndarray, lens, sample: int) -> dict:
+    """Bit-for-bit comparison on the sample: the same (position, column) set and the same
+    score bits."""
+    a = np.sort(restrict_to_sample(gpu_hits, lens, sample), order=["pos", "col"])
+    b = np.sort(oracle_hits, order=["pos", "col"])
+    same = (len(a) == len(b) and np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["col"], b["col"])
+            and np.array_equal(a["score"].view(np.uint32), b["score"].view(np.uint32)))
+    return {"positions": int(sample), "hits": int(len(b)), "gpu_hits": int(len(a)), "identical": bool(same)}
+
+
+def product_libraries_loaded() -> list[str]:
+    """This process's mapped shared libraries that belong to the product (blamm_gb300/)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return ["unknown: /proc/self/maps unreadable"]
+    pkg = os.path.realpath(os.path.join(ROOT, "blamm_gb300"))
+    return sorted(p for p in paths if os.path.realpath(p).startswith(pkg))
+
+
+def cli_e2e(wl, bases, sample: int) -> dict:
+    """The reference's command line on the CPU sample, end to end: FASTA in, occurrence file
+    out, `scan -rc -pt 1e-4 -t <cores>` through the oracle's port of the reference's CLI on its
+    BLAS block loop (OpenBLAS, one BLAS thread per worker).  `dict` is written directly (the
+    sample's sequences with the whole genome's base counts, so that the PWMs are the headline's)
+    and `hist` runs untimed beforehand, as the reference's own workflow runs them once."""
+    import shutil
+    import subprocess
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from blamm_gb300 import workloads
+    blas = oracle.find_blas()
+    if not os.path.exists(oracle.CLI_PATH) or not blas:
+        return {"unavailable": "oracle CLI or an LP64 BLAS missing"}
+    d = tempfile.mkdtemp(prefix="blamm_cli_")
+    try:
+        seqs, left = [], sample
+        for name, s in wl.sequences:
+            if left <= 0:
+                break
+            seqs.append((name, s[:left]))
+            left -= len(s[:left])
+        workloads.write_fasta(os.path.join(d, "sample.fa"), seqs)
+        with open(os.path.join(d, "sequences.mf"), "w") as f:
+            f.write("genome\tsample.fa\n")
+        workloads.write_jaspar(os.path.join(d, "motifs.jaspar"), wl.motifs)
+        workloads.write_settings(os.path.join(d, "settings.cnf"))
+        counts = [int(np.count_nonzero((bases | 0x20) == ord(c))) for c in "acgt"]
+        with open(os.path.join(d, "sequences.mf.dict"), "w") as f:
+            f.write(f"NUM_SPECIES\t1\nSPECIES\tgenome\nNUM_FASTA_FILES\t1\nsample.fa\n"
+                    f"TOT_SEQ_LENGTH\t{sample}\nNUCL_COUNT_ACGT\t" + "\t".join(map(str, counts)) +
+                    f"\nNUM_SEQUENCES\t{len(seqs)}\n" + "".join(n + "\n" for n, _ in seqs))
+        env = dict(os.environ, OPENBLAS_NUM_THREADS="1", BLAMM_ORACLE_BLAS=blas)
+        subprocess.run([oracle.CLI_PATH, "hist", "motifs.jaspar", "sequences.mf"], cwd=d, env=env, check=True,
+                       stdout=subprocess.DEVNULL)
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        subprocess.run([oracle.CLI_PATH, "scan", "-rc", "-pt", str(wl.pvalue), "-t", str(cores), "motifs.jaspar",
+                        "sequences.mf"], cwd=d, env=env, check=True, stdout=subprocess.DEVNULL)
+        dt = time.perf_counter() - t0
+        with open(os.path.join(d, "occurrences.txt"), "rb") as f:
+            lines = sum(1 for _ in f)
+        return {"value": sample * 2 * len(wl.motifs) / dt, "unit": UNIT, "seconds": dt, "cores": cores,
+                "occurrence_lines": lines,
+                "sample": f"first {sample} bp (FASTA, {len(seqs)} sequences) x {2 * len(wl.motifs)} columns: "
+                          "read, scan, write the occurrence file"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def cpu_model() -> str:
@@ -205,17 +313,18 @@ def run_reference(a, rank, world):
     """--impl reference: the reference's CPU scan (oracle port of its BLAS loop) per step."""
     if rank != 0:
         return
-    wl, bases, runs, rseq, P, lens, thr = build_workload(a.seed, a.bases)
+    wl, bases, runs, rseq, P, lens, thr, colkey = build_workload_oracle(a.seed, a.bases)
     sample = min(a.cpu_sample, len(bases))
     for _ in range(a.warmup):
         cpu_sample_scan(bases, runs, P, lens, thr, sample)
     vals, times = [], []
-    cores = 1
+    cores, hits = 1, None
     for _ in range(a.steps):
-        v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, sample)
+        v, cores, dt, hits = cpu_sample_scan(bases, runs, P, lens, thr, sample)
         vals.append(v)
         times.append(dt)
     value = float(np.mean(vals))
+    cli = cli_e2e(wl, bases, sample)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
@@ -227,6 +336,12 @@ def run_reference(a, rank, world):
                          "sample": f"first {sample} bp of the stream x 1024 columns, "
                                    "the reference's BLAS block loop (h=1000, w=250) on OpenBLAS"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        # the sample's hits keyed by (position, PFM, strand, score bits): the GPU arm prints the
+        # same digest of its headline hits restricted to the sample
+        "sample_hits": sample_digest(hits, colkey) if hits is not None else None,
+        "cli_e2e": cli,
+        "setup": "motif bank, PWMs and p-value thresholds from the oracle",
+        "product_libraries_loaded": product_libraries_loaded(),
     }
     print(json.dumps(line), flush=True)
 
@@ -399,6 +514,14 @@ def run_genome_1gbp(a):
             st = ts[-1]
             h = d_h[: nh * HD.itemsize].cpu().numpy().view(HD)
             digests[mode] = hit_digest(h)
+            if mode == "bf16x2":
+                # parity on a sample of this workload: the oracle's scan of the first bases
+                # (Markov background, N runs) against the GPU hits of the windows inside them
+                sys.path.insert(0, os.path.join(ROOT, "oracle"))
+                import oracle
+                smp = min(n, a.cpu_sample // 4)
+                oh = oracle.scan(bases[:smp], runs[runs < smp], P, lens, thr[pi], nthreads=os.cpu_count() or 8)
+                res["parity_vs_oracle"] = parity_vs_oracle(h, oh, lens, smp)
             kern = float(np.median([t["scan_ms"] for t in ts]))
             tot = float(np.median([t["kernel_ms"] for t in ts]))
             res[mode] = {"hits": int(nh), "candidates": int(st["candidates"]), "scan_kernel_ms": kern,
@@ -522,9 +645,9 @@ def run_ours(a, rank, world, local):
             t = torch.from_numpy(c.astype(np.int64)).to(f"cuda:{local}")
             dist.all_reduce(t, op=dist.ReduceOp.SUM)
             return t.cpu().numpy().astype(np.uint64)
-        wl, bases, runs, rseq, P, lens, thr = build_workload(a.seed, a.bases, rank, genome_counts)
+        wl, bases, runs, rseq, P, lens, thr, colkey = build_workload(a.seed, a.bases, rank, genome_counts)
     else:
-        wl, bases, runs, rseq, P, lens, thr = build_workload(a.seed, a.bases)
+        wl, bases, runs, rseq, P, lens, thr, colkey = build_workload(a.seed, a.bases)
     n, ncols = len(bases), P.shape[0]
     units = n * ncols
     flops_per_bp = float(8 * lens.astype(np.int64).sum())
@@ -591,7 +714,8 @@ def run_ours(a, rank, world, local):
         total_units = float(units)
     value = total_units / (step_ms / 1e3)
     st = sc.stats()
-    ref_digest = hit_digest(hits_on_device(nh))
+    headline_hits = hits_on_device(nh)
+    ref_digest = hit_digest(headline_hits)
 
     # ---- the same step end to end through host buffers (pinned)
     lib = gpu_lib()
@@ -701,7 +825,12 @@ def run_ours(a, rank, world, local):
             line["serve_p50_ms"] = line["serve"]["open_loop"][-1]["p50_ms"]
             line["serve_p99_ms"] = line["serve"]["open_loop"][-1]["p99_ms"]
     if rank == 0 and world == 1:
-        v, cores, dt, _ = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
+        v, cores, dt, ohits = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
+        # parity on the headline workload: the GPU headline hits of every window inside the sample
+        # against the oracle's port of the reference's BLAS loop, bit for bit
+        smp = min(a.cpu_sample, n)
+        line["parity_vs_oracle"] = parity_vs_oracle(headline_hits, ohits, lens, smp)
+        line["sample_hits"] = sample_digest(restrict_to_sample(headline_hits, lens, smp), colkey)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                                 "sample": f"first {min(a.cpu_sample, n)} bp x {ncols} columns in {dt:.1f} s: the "
                                           "reference's BLAS block loop (h=1000, w=250, OpenBLAS sgemm per tile "

@@ -110,6 +110,42 @@ def matrix_tiles(lens, min_zero_area: int) -> np.ndarray:
     return out[:n]
 
 
+def motif_bank(pfms, bg_counts, pseudo: float = 0.25, pvalues=(1e-4,), nbins: int = 250,
+               max_length: int = 10_000_000, revcompl: bool = True):
+    """The reference's scan set-up for a list of PFMs, restated with the oracle's functions:
+    motifs ordered by length (the sort in MotifContainer::loadCBMotifs / loadJasparMotifs,
+    motif.cpp:367, 436), each followed by its reverse complement (addReverseComplements,
+    motif.cpp:439-449), PWMs from the dictionary's base counts (PFM2PWM, motif.cpp:194-223),
+    the matrix P (generateMatrix, motif.cpp:542-564) and per p-value thresholds from the
+    theoretical histogram of each forward motif (hist.cpp:162-175, getScoreCutoff
+    motif.cpp:47-69; a reverse complement shares its forward motif's histogram file,
+    pwmscan.cpp:599-616).
+
+    Returns (P (ncols x 4*Lmax), lengths, thresholds (len(pvalues) x ncols), column_motif,
+    column_strand): column c scores PFM column_motif[c] on strand column_strand[c] (0 = +)."""
+    order = sorted(range(len(pfms)), key=lambda i: np.asarray(pfms[i]).shape[0])
+    bgp = nucl_prob(bg_counts, pseudo)
+    cols = []
+    for i in order:
+        pfm = np.asarray(pfms[i])
+        fwd = pfm2pwm(pfm, bg_counts, pseudo, False)
+        mn, mx = min_max_score(fwd)
+        width = np.float32(np.float32(mx) - np.float32(mn)) / np.float32(nbins)
+        h = theoretical_hist(fwd, bgp, nbins, max_length)
+        t = [score_cutoff(h, mn, float(width), mx, pv) for pv in pvalues]
+        cols.append((fwd, i, 0, t))
+        if revcompl:
+            cols.append((pfm2pwm(revcompl_pfm(pfm), bg_counts, pseudo, True), i, 1, t))
+    lmax = max(c[0].shape[0] for c in cols)
+    P = np.zeros((len(cols), 4 * lmax), dtype=np.float32)
+    for c, (pwm, _, _, _) in enumerate(cols):
+        P[c, :pwm.size] = pwm.ravel()
+    lens = np.array([c[0].shape[0] for c in cols], dtype=np.int32)
+    thr = np.array([c[3] for c in cols], dtype=np.float32).T.copy()
+    return (P, lens, thr, np.array([c[1] for c in cols], dtype=np.int64),
+            np.array([c[2] for c in cols], dtype=np.int8))
+
+
 def scan(bases: np.ndarray, run_start: np.ndarray, P: np.ndarray, col_len, thr,
          nthreads: int = 8, lower_scores: bool = False) -> np.ndarray:
     """Sequential-FP32 scan (the reference's hit set). P: (ncols, p_rows).

@@ -612,12 +612,32 @@ static int run_scan(int argc, char **argv)
         if (orc_stream_read((const char *const *)sp[s].files, sp[s].nfiles, (int64_t)sp[s].tot,
                             &str, err, sizeof err))
             die(err);
-        int64_t nh = orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len,
-                                 thr, nthreads, simple, NULL, 0);
+        /* The reference's default scan is its BLAS block loop (pwmscan.cpp:223-278); it runs
+         * here when BLAMM_ORACLE_BLAS names an LP64 BLAS library with sgemm_, else the
+         * sequential scorer, which gives the same hits (motif.cpp:225-239). */
+        const char *blas = getenv("BLAMM_ORACLE_BLAS");
+        int use_blas = !simple && blas && *blas;
+        if (use_blas && orc_set_blas(blas)) die("BLAMM_ORACLE_BLAS: cannot load sgemm");
+        int32_t *tiles = NULL;
+        int ntiles = 0;
+        if (use_blas) {
+            tiles = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(2 * ncols + 4));
+            ntiles = orc_matrix_tiles(len, ncols, st.tile_min_zero_area, tiles, 2 * ncols + 4);
+        }
+        int64_t nh = use_blas ? orc_scan_blas(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols,
+                                              len, thr, tiles, ntiles, (int)st.s_h, (int)st.s_w,
+                                              nthreads, NULL, 0)
+                              : orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len,
+                                            thr, nthreads, simple, NULL, 0);
         if (nh < 0) die("oracle scan failed");
         orc_hit *hits = (orc_hit *)malloc(sizeof(orc_hit) * (size_t)(nh ? nh : 1));
-        orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len, thr, nthreads,
-                    simple, hits, nh);
+        if (use_blas)
+            orc_scan_blas(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len, thr, tiles,
+                          ntiles, (int)st.s_h, (int)st.s_w, nthreads, hits, nh);
+        else
+            orc_scan_ex(str.bases, str.n, str.run_start, str.nruns, P, rows, ncols, len, thr, nthreads,
+                        simple, hits, nh);
+        free(tiles);
         int64_t r = 0;
         for (int64_t h = 0; h < nh; h++) {
             int64_t p = hits[h].pos;

@@ -297,3 +297,29 @@ def test_bench_reference_arm_prints_the_contract_line():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    # the arm runs the oracle only: no product library in the process
+    assert line["product_libraries_loaded"] == []
+    assert line["sample_hits"]["hits"] > 0
+    assert line["cli_e2e"]["value"] > 0 and line["cli_e2e"]["occurrence_lines"] > 0
+
+
+def test_oracle_bank_equals_product_bank():
+    """The oracle's restatement of the reference's scan set-up (used by the benchmark's
+    reference arm) gives the product's motif bank: per (PFM, strand) the same PWM bits, length
+    and p-value thresholds."""
+    from blamm_gb300 import workloads
+    rng = np.random.default_rng(5)
+    pfms = [p for _, p in workloads.random_pfms(rng, 40, 5, 30)]
+    counts = np.array([2900, 2100, 2100, 2900], dtype=np.uint64)
+    P, lens, thr, cmot, cstr = oracle.motif_bank(pfms, counts, 0.25, (1e-4, 1e-5))
+    bank = MotifBank.from_pfms(pfms, revcompl=True)
+    bank.generate(counts, 0.25)
+    Pb, lb, rcb = bank.matrix()
+    bgp = oracle.nucl_prob(counts, 0.25)
+    tb = [bank.pvalue_thresholds(bgp, pv, 250, 10_000_000) for pv in (1e-4, 1e-5)]
+    assert np.all(np.diff(lens) >= 0)
+    got = {(int(cmot[c]), int(cstr[c])): (P[c, :4 * lens[c]].tobytes(), thr[0][c], thr[1][c])
+           for c in range(len(lens))}
+    want = {(int(bank.name(c)[1:]), int(rcb[c])): (Pb[c, :4 * lb[c]].tobytes(), tb[0][c], tb[1][c])
+            for c in range(len(lb))}
+    assert got == want
