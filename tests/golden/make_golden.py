@@ -109,8 +109,9 @@ def case_cb(d):
 
 
 def case_two_sequences_1mbp(d):
-    """The two-sequence shapes at reduced size: 32 motifs (L 6-20), 2 x 100 kbp iid (A=T=0.3), -rc -pt 1e-4."""
-    wl = workloads.two_sequences_1mbp(0, seq_len=100_000)
+    """The two-sequence case at full size: 32 motifs (L 6-20), 2 x 500 kbp iid (A=T=0.3), -rc -pt 1e-4.
+    The FASTA file and the occurrence file are stored gzip-compressed (see COMPRESS)."""
+    wl = workloads.two_sequences_1mbp(0, seq_len=500_000)
     os.makedirs(os.path.join(d, "seqs"), exist_ok=True)
     workloads.write_fasta(os.path.join(d, "seqs", "seqs.fa"), wl.sequences)
     with open(os.path.join(d, "sequences.mf"), "w") as f:
@@ -126,6 +127,18 @@ def case_two_sequences_1mbp(d):
 
 
 CASES = {"mixed": case_mixed, "cb": case_cb, "two_sequences_1mbp": case_two_sequences_1mbp}
+
+# files kept gzip-compressed in the fixtures (tests/golden_cases.py inflates them)
+COMPRESS = {"two_sequences_1mbp": ["seqs/seqs.fa", "expected/occ_pt.txt"]}
+
+
+def compress(d, files):
+    import gzip
+    for f in files:
+        p = os.path.join(d, f)
+        with open(p, "rb") as fi, gzip.GzipFile(p + ".gz", "wb", compresslevel=9, mtime=0) as fo:
+            shutil.copyfileobj(fi, fo)
+        os.remove(p)
 
 
 def run_reference(d, spec):
@@ -174,6 +187,7 @@ def main():
         spec = fn(d)
         run_reference(d, spec)
         collect(d, spec)
+        compress(d, COMPRESS.get(name, []))
         with open(os.path.join(d, "case.json"), "w") as f:
             json.dump(spec, f, indent=1)
         print(name, "ok")

@@ -2,8 +2,8 @@ set output "hist_cfg1_MOTIF00008.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-50.5185:14.7549]
-set yrange [0:2105]
+set xrange [-50.5169:14.7526]
+set yrange [0:2099]
 set xlabel 'PWM score'
 set ylabel 'count'
 plot "hist_cfg1_MOTIF00008.dat" using 1:2 title 'MOTIF00008 (cfg1)' with boxes

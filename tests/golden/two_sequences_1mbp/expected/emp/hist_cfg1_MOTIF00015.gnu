@@ -2,7 +2,7 @@ set output "hist_cfg1_MOTIF00015.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-33.4968:13.0586]
+set xrange [-33.4977:13.0602]
 set yrange [0:2030]
 set xlabel 'PWM score'
 set ylabel 'count'

@@ -2,7 +2,7 @@ set output "hist_cfg1_MOTIF00020.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-26.0731:7.46311]
+set xrange [-26.0741:7.46691]
 set yrange [0:1919]
 set xlabel 'PWM score'
 set ylabel 'count'

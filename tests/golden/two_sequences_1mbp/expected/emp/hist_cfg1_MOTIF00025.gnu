@@ -2,8 +2,8 @@ set output "hist_cfg1_MOTIF00025.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-82.2156:20.9641]
-set yrange [0:2446]
+set xrange [-82.2118:20.9675]
+set yrange [0:2448]
 set xlabel 'PWM score'
 set ylabel 'count'
 plot "hist_cfg1_MOTIF00025.dat" using 1:2 title 'MOTIF00025 (cfg1)' with boxes

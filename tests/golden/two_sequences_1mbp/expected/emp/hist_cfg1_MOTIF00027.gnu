@@ -2,8 +2,8 @@ set output "hist_cfg1_MOTIF00027.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-34.3549:10.8915]
-set yrange [0:1822]
+set xrange [-34.3554:10.8939]
+set yrange [0:1800]
 set xlabel 'PWM score'
 set ylabel 'count'
 plot "hist_cfg1_MOTIF00027.dat" using 1:2 title 'MOTIF00027 (cfg1)' with boxes

@@ -2,8 +2,8 @@ set output "hist_cfg1_MOTIF00017.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-91.5378:26.3644]
-set yrange [0:184815]
+set xrange [-91.5308:26.3759]
+set yrange [0:185088]
 set xlabel 'PWM score'
 set ylabel 'count'
 plot "hist_cfg1_MOTIF00017.dat" using 1:2 title 'MOTIF00017 (cfg1)' with boxes

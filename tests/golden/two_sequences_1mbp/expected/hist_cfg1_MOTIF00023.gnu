@@ -2,8 +2,8 @@ set output "hist_cfg1_MOTIF00023.ps"
 set key autotitle columnhead
 set terminal postscript landscape
 set terminal postscript noenhanced
-set xrange [-32.1111:9.82895]
-set yrange [0:119814]
+set xrange [-32.1134:9.83792]
+set yrange [0:122504]
 set xlabel 'PWM score'
 set ylabel 'count'
 plot "hist_cfg1_MOTIF00023.dat" using 1:2 title 'MOTIF00023 (cfg1)' with boxes

@@ -1,6 +1,7 @@
 """Running a golden case (tests/golden/<case>) with some `blamm`-compatible binary."""
 from __future__ import annotations
 
+import gzip
 import json
 import os
 import shutil
@@ -21,6 +22,13 @@ def stage(case: str, tmp: str) -> str:
     src = os.path.join(GOLDEN, case)
     dst = os.path.join(tmp, case)
     shutil.copytree(src, dst, ignore=shutil.ignore_patterns("expected", "case.json"))
+    for root, _, files in os.walk(dst):  # inputs stored gzip-compressed are inflated
+        for f in files:
+            if f.endswith(".gz"):
+                p = os.path.join(root, f)
+                with gzip.open(p, "rb") as fi, open(p[:-3], "wb") as fo:
+                    shutil.copyfileobj(fi, fo)
+                os.remove(p)
     os.makedirs(os.path.join(dst, "emp"), exist_ok=True)
     return dst
 
@@ -38,14 +46,18 @@ def run(binary: str, d: str, spec: dict, skip=(), env=None, extra_scan=()) -> No
 
 
 def sorted_lines(path: str) -> list[bytes]:
-    with open(path, "rb") as f:
+    opener = gzip.open if path.endswith(".gz") else open
+    with opener(path, "rb") as f:
         return sorted(f.read().splitlines(keepends=True))
 
 
 def compare(d: str, case: str, spec: dict, what=("dict", "hist", "thresholds", "occ", "emp")) -> None:
     exp = os.path.join(GOLDEN, case, "expected")
     for f in sorted(os.listdir(exp)):
-        e, g = os.path.join(exp, f), os.path.join(d, f)
+        e = os.path.join(exp, f)
+        if f.endswith(".gz"):  # a compressed expected file: compared with the uncompressed output
+            f = f[:-3]
+        g = os.path.join(d, f)
         if f == "emp":
             if "emp" in what:
                 for h in sorted(os.listdir(e)):
