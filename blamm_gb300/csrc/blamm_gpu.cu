@@ -100,8 +100,8 @@ struct blamm_ctx {
     size_t cap_e16 = 0;
     int64_t *d_runs = nullptr;
     size_t cap_runs = 0;
-    unsigned long long *d_cand = nullptr;
-    int64_t cand_cap = 0;
+    uint4 *d_cand = nullptr;  // candidate record slots (scan_tc.cuh: blocks of kRecBlock)
+    int64_t cand_cap = 0;     // record slots
     blamm_hit *d_hits = nullptr;
     int64_t hits_cap = 0;
     unsigned long long *d_counters = nullptr;  // [0] candidates, [1] hits
@@ -127,6 +127,7 @@ struct blamm_ctx {
     int prof_ctas = 0;
 
     blamm_stats stats{};
+    int64_t rec_slots = 0;  // record slots the last tensor-core scan reserved
 };
 
 // ------------------------------------------------------------------ errors
@@ -228,9 +229,7 @@ static int build_plan(blamm_ctx *ctx, int terms)
     const int erows_all = kBM + 4 * gmax_all + 8;
     const long long smem_limit = (long long)ctx->max_smem;
     // everything but the B tiles (E stages, bias A tile, candidate staging, ...)
-    const long long other = (long long)kEStages * erows_all * 16 + 4096 +
-                            (long long)kEpiWarps * kCandBuf * 8 + 256LL * sizeof(TileDesc) + 64 + 128 + 64 + 2048 +
-                            1024;
+    const long long other = (long long)tc_smem_layout(0u, terms, erows_all, 256).total;
     const long long b_term_cap = (smem_limit - other) / terms;
     const int ncap = std::max(32, std::min(256, ctx->plan_nmax / 32 * 32));
     // widest tile whose B terms (g motif k-steps + 1 bias k-step) fit shared memory
@@ -651,6 +650,58 @@ static TcParams tc_params(const blamm_ctx *ctx, const uint4 *e16, int64_t n)
     return p;
 }
 
+// The scan kernel counts jobs and record slots in 32 bits.
+constexpr int64_t kMaxJobs = 0x7fffffff;
+constexpr int64_t kMaxRecordSlots = (int64_t(1) << 31) - 1024;
+
+static int check_jobs(blamm_ctx *ctx, long long njobs)
+{
+    return njobs > kMaxJobs ? fail(ctx, BLAMM_ERR_UNSUPPORTED,
+                                   "%lld scan jobs (tiles x 128-position blocks) exceed one launch's %lld; "
+                                   "scan the stream in parts", njobs, (long long)kMaxJobs)
+                            : BLAMM_OK;
+}
+
+// Record slots a scan with this grid reserves beyond its records: every drain warp holds
+// one block it fills and one reserved ahead.
+static int64_t record_slots_reserved(int grid) { return (int64_t)grid * kEpiWarps * 2 * kRecBlock; }
+
+// Record slots for a first scan of n positions (about one candidate per 1000 position x
+// column pairs, the thresholds' p-values being small) on a full grid.
+static int64_t record_slots_guess(const blamm_ctx *ctx, int64_t n, double per = 1000.0)
+{
+    const double est = (double)n * scanned_columns(ctx) / per + (double)record_slots_reserved(ctx->sm_count);
+    return (int64_t)std::min(std::max(est, (double)(1 << 20)), 512.0 * 1024 * 1024);
+}
+
+// Rescoring of the candidate records of one scan: the context's bank and chunk filter.
+static RescoreParams rescore_params(const blamm_ctx *ctx, const uint4 *cand, const unsigned long long *cand_count,
+                                    int64_t cand_cap, const uint32_t *seq2,
+                                    const uint32_t *zmask, int64_t n, const int64_t *d_runs, int64_t nruns,
+                                    blamm_hit *d_hits, unsigned long long *hit_count, int64_t hit_cap)
+{
+    RescoreParams r{};
+    r.cand = cand;
+    r.slot_col = ctx->d_slot_col;
+    r.cand_count = cand_count;
+    r.cand_cap = cand_cap;
+    r.seq2 = seq2;
+    r.zmask = zmask;
+    r.n = n;
+    r.run_start = d_runs;
+    r.nruns = nruns;
+    r.P = ctx->d_P;
+    r.p_rows = ctx->p_rows;
+    r.col_len = ctx->d_len;
+    r.thr = ctx->d_thr;
+    r.hits = d_hits;
+    r.hit_count = hit_count;
+    r.hit_cap = hit_cap;
+    r.keep_below = ctx->keep_below;
+    r.pos_base = ctx->pos_base;
+    return r;
+}
+
 // One launch of the scan kernel instance that p asks for.
 template <bool kDump, bool kProf>
 static void launch_tc_as(const TcParams &p, int grid, uint32_t smem, cudaStream_t st)
@@ -674,11 +725,10 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     if (rc) return rc;
     const int64_t n_mtiles = (n + kBM - 1) / kBM;
     const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    if ((rc = check_jobs(ctx, njobs))) return rc;
     if (ctx->cand_cap == 0) {
-        const double est = (double)n * ctx->ncols / 1000.0;
-        int64_t want = (int64_t)std::min(std::max(est, (double)(1 << 20)), 512.0 * 1024 * 1024);
         size_t cap = 0;
-        rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)want);
+        rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)record_slots_guess(ctx, n));
         if (rc) return rc;
         ctx->cand_cap = (int64_t)cap;
     }
@@ -694,6 +744,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
         TcParams p = tc_params(ctx, ctx->d_e16, n);
         p.cand = ctx->d_cand;
         p.cand_count = ctx->d_counters;
+        p.ncand = ctx->d_counters + 3;
         p.cand_cap = ctx->cand_cap;
         p.status = ctx->d_status;
         p.wait_limit = ctx->wait_limit;
@@ -728,38 +779,27 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
             CK(cudaMemcpy(ctx->prof.data(), ctx->d_prof, sizeof(long long) * 32 * grid, cudaMemcpyDeviceToHost));
             ctx->prof_ctas = grid;
         }
-        ctx->stats.candidates = (int64_t)ncand;
+        ctx->stats.candidates = 0;  // counted by the rescoring
+        ctx->rec_slots = (int64_t)ncand;
         if ((int64_t)ncand <= ctx->cand_cap) break;
         // grow and re-run
         size_t cap = 0;
         CK(cudaFreeAsync(ctx->d_cand, ctx->stream));
         ctx->d_cand = nullptr;
         ctx->cand_cap = 0;
-        rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)(ncand + ncand / 4 + 1024));
+        if ((int64_t)ncand >= kMaxRecordSlots)
+            return fail(ctx, BLAMM_ERR_OVERFLOW, "%llu candidate records exceed one launch's %lld", ncand,
+                        (long long)kMaxRecordSlots);
+        rc = ensure(ctx, &ctx->d_cand, &cap,
+                    (size_t)std::min<int64_t>((int64_t)(ncand + ncand / 4 + 1024), kMaxRecordSlots));
         if (rc) return rc;
         ctx->cand_cap = (int64_t)cap;
         if (attempt == 2) return fail(ctx, BLAMM_ERR_OVERFLOW, "candidate buffer overflow");
     }
-    RescoreParams r{};
-    r.cand = ctx->d_cand;
-    r.slot_col = ctx->d_slot_col;
-    r.cand_count = ctx->d_counters;
-    r.cand_cap = ctx->cand_cap;
-    r.seq2 = ctx->d_seq2;
-    r.zmask = ctx->d_zmask;
-    r.n = n;
-    r.run_start = d_runs;
-    r.nruns = nruns;
-    r.P = ctx->d_P;
-    r.p_rows = ctx->p_rows;
-    r.col_len = ctx->d_len;
-    r.thr = ctx->d_thr;
-    r.hits = d_hits;
-    r.hit_count = ctx->d_counters + 1;
-    r.hit_cap = hit_cap;
-    r.keep_below = ctx->keep_below;
-    r.pos_base = ctx->pos_base;
-    const int64_t nc = ctx->stats.candidates;
+    const RescoreParams r = rescore_params(ctx, ctx->d_cand, ctx->d_counters, ctx->cand_cap,
+                                           ctx->d_seq2, ctx->d_zmask, n, d_runs, nruns, d_hits,
+                                           ctx->d_counters + 1, hit_cap);
+    const int64_t nc = ctx->rec_slots;
     if (nc > 0) {
         const int threads = 256;
         const int64_t blocks = std::min<int64_t>((nc + threads - 1) / threads, (int64_t)ctx->sm_count * 16);
@@ -851,9 +891,11 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     else rc = run_tc(ctx, n, d_runs, nruns, d_hits, hit_cap, nullptr, 0, 0, &launches);
     if (rc) return rc;
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-    unsigned long long nh = 0;
-    CK(cudaMemcpyAsync(&nh, ctx->d_counters + 1, sizeof nh, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long cnt[4] = {0, 0, 0, 0};  // record slots, hits, -, candidates
+    CK(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    const unsigned long long nh = cnt[1];
+    if (ctx->mode != BLAMM_MODE_FP32) ctx->stats.candidates = (int64_t)cnt[3];
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
     ctx->stats.kernel_ms = ms;
@@ -992,15 +1034,19 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
     }
     launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
     CK(cudaGetLastError());
-    CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));      // record slots of this chunk
+    CK(cudaMemsetAsync(cnt + 3, 0, sizeof(unsigned long long), ctx->stream));  // its candidates
     const int64_t n_mtiles = (n + kBM - 1) / kBM;
     const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    int rc = check_jobs(ctx, njobs);
+    if (rc) return rc;
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
     TcParams p = tc_params(ctx, ctx->d_e16, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
+    p.ncand = cnt + 3;
     p.cand_cap = ctx->cand_cap;
     p.status = ctx->d_status;
     p.wait_limit = ctx->wait_limit;
@@ -1008,25 +1054,8 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
     const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
     launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
     CK(cudaGetLastError());
-    RescoreParams r{};
-    r.cand = ctx->d_cand;
-    r.slot_col = ctx->d_slot_col;
-    r.cand_count = cnt;
-    r.cand_cap = ctx->cand_cap;
-    r.seq2 = ctx->d_seq2;
-    r.zmask = ctx->d_zmask;
-    r.n = n;
-    r.run_start = d_runs;
-    r.nruns = nruns;
-    r.P = ctx->d_P;
-    r.p_rows = ctx->p_rows;
-    r.col_len = ctx->d_len;
-    r.thr = ctx->d_thr;
-    r.hits = d_hits;
-    r.hit_count = cnt + 1;
-    r.hit_cap = hit_cap;
-    r.keep_below = ctx->keep_below;
-    r.pos_base = ctx->pos_base;
+    const RescoreParams r = rescore_params(ctx, ctx->d_cand, cnt, ctx->cand_cap, ctx->d_seq2, ctx->d_zmask,
+                                           n, d_runs, nruns, d_hits, cnt + 1, hit_cap);
     rescore_kernel<<<(unsigned)(ctx->sm_count * 8), 256, 0, ctx->stream>>>(r);
     CK(cudaGetLastError());
     return BLAMM_OK;
@@ -1058,8 +1087,7 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
         if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(span)))) return rc;
         // candidates: four times the usual first guess for a chunk (a chunk that still
         // overflows sends the whole call to the synchronous path)
-        const double want = std::min(std::max((double)span * scanned_columns(ctx) / 250.0, (double)(1 << 20)),
-                                     512.0 * 1024 * 1024);
+        const double want = (double)record_slots_guess(ctx, span, 250.0);
         if ((double)ctx->cand_cap < want) {
             size_t cap = ctx->cand_cap > 0 ? (size_t)ctx->cand_cap : 0;
             if ((rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)want))) return rc;
@@ -1145,8 +1173,9 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
                            hit_cap);
         ctx->keep_below = ctx->pos_base = 0;
         if (rc) return rc;
-        // this chunk's candidate count, the running hit count and the status, to host memory
-        CK(cudaMemcpyAsync(hc_k + 4 * k, ctx->d_counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        // this chunk's record slots, the running hit count, its candidates and the status, to
+        // host memory
+        CK(cudaMemcpyAsync(hc_k + 4 * k, ctx->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            ctx->stream));
         CK(cudaMemcpyAsync(hc_k + 4 * k + 2, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaEventRecord(ctx->done_ev[b], ctx->stream));
@@ -1163,7 +1192,7 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
     int status = 0;
     for (int64_t k = 0; k < nchunks; ++k) {
         const int64_t nc = (int64_t)hc_k[4 * k];
-        if (tc) total.candidates += nc;
+        if (tc) total.candidates += (int64_t)hc_k[4 * k + 3];
         if (tc && nc > ctx->cand_cap) *cand_overflow = std::max(*cand_overflow, nc);
         status |= (int)(hc_k[4 * k + 2] & 0xffffffffu);
     }
@@ -1485,13 +1514,13 @@ namespace {
 
 constexpr int64_t kStaticMaxBases = int64_t(4) << 20;  // positions per call
 constexpr int64_t kStaticWords32 = (kStaticMaxBases + kStreamPad + 31) / 32;
-constexpr int64_t kStaticCandCap = int64_t(1) << 20;   // tensor-core candidates per call
+constexpr int64_t kStaticCandCap = int64_t(2) << 20;   // tensor-core candidate record slots per call
 constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kStaticSeq2Off = 0;
 constexpr size_t kStaticZmaskOff = round256(kStaticSeq2Off + sizeof(uint32_t) * 2 * kStaticWords32);
 constexpr size_t kStaticE16Off = round256(kStaticZmaskOff + sizeof(uint32_t) * kStaticWords32);
 constexpr size_t kStaticCandOff = round256(kStaticE16Off + sizeof(uint4) * (kStaticMaxBases + kStreamPad));
-constexpr size_t kStaticCountOff = round256(kStaticCandOff + sizeof(unsigned long long) * kStaticCandCap);
+constexpr size_t kStaticCountOff = round256(kStaticCandOff + sizeof(uint4) * kStaticCandCap);
 constexpr size_t kStaticStatusOff = round256(kStaticCountOff + sizeof(unsigned long long) * 4);
 constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 73 MiB
 
@@ -1533,9 +1562,6 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
     if (n > kStaticMaxBases)
         return fail(ctx, BLAMM_ERR_ARG, "blamm_scan_device_static: %lld positions > the static limit %lld",
                     (long long)n, (long long)kStaticMaxBases);
-    if (n == 0) return BLAMM_OK;
-    if (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits))
-        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
     if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
     const bool tc = ctx->mode != BLAMM_MODE_FP32;
     const int terms = mode_terms(ctx);
@@ -1543,6 +1569,9 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         return fail(ctx, BLAMM_ERR_STATE,
                     "blamm_scan_device_static: no tensor-core plan for this bank, mode and thresholds "
                     "(one blamm_scan or blamm_scan_device call builds it)");
+    if (n == 0) return BLAMM_OK;
+    if (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits))
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
     CK(cudaSetDevice(ctx->device));
     unsigned char *base = nullptr;
     int rc = static_scratch(ctx, &base);
@@ -1550,7 +1579,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
     uint32_t *seq2 = reinterpret_cast<uint32_t *>(base + kStaticSeq2Off);
     uint32_t *zmask = reinterpret_cast<uint32_t *>(base + kStaticZmaskOff);
     uint4 *e16 = reinterpret_cast<uint4 *>(base + kStaticE16Off);
-    unsigned long long *cand = reinterpret_cast<unsigned long long *>(base + kStaticCandOff);
+    uint4 *cand = reinterpret_cast<uint4 *>(base + kStaticCandOff);
     unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + kStaticCountOff);
     int *status = reinterpret_cast<int *>(base + kStaticStatusOff);
 
@@ -1586,6 +1615,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         TcParams p = tc_params(ctx, e16, n);
         p.cand = cand;
         p.cand_count = counters;
+        p.ncand = counters + 3;
         p.cand_cap = kStaticCandCap;
         p.status = status;
         p.wait_limit = ctx->wait_limit;
@@ -1600,29 +1630,13 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         CK(cudaMemcpyAsync(&st, status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         if (st) return fail(ctx, BLAMM_ERR_TIMEOUT, "scan kernel: a device wait timed out");
-        ctx->stats.candidates = (int64_t)ncand;
         if ((int64_t)ncand > kStaticCandCap)
             return fail(ctx, BLAMM_ERR_OVERFLOW,
-                        "blamm_scan_device_static: %llu candidates > the static limit %lld (scan fewer "
-                        "positions per call)", ncand, (long long)kStaticCandCap);
+                        "blamm_scan_device_static: %llu candidate record slots > the static limit %lld (scan "
+                        "fewer positions per call)", ncand, (long long)kStaticCandCap);
         if (ncand > 0) {
-            RescoreParams r{};
-            r.cand = cand;
-            r.slot_col = ctx->d_slot_col;
-            r.cand_count = counters;
-            r.cand_cap = kStaticCandCap;
-            r.seq2 = seq2;
-            r.zmask = zmask;
-            r.n = n;
-            r.run_start = d_run_start;
-            r.nruns = nruns;
-            r.P = ctx->d_P;
-            r.p_rows = ctx->p_rows;
-            r.col_len = ctx->d_len;
-            r.thr = ctx->d_thr;
-            r.hits = d_hits;
-            r.hit_count = counters + 1;
-            r.hit_cap = hit_cap;
+            const RescoreParams r = rescore_params(ctx, cand, counters, kStaticCandCap, seq2, zmask, n,
+                                                   d_run_start, nruns, d_hits, counters + 1, hit_cap);
             const int threads = 256;
             const int64_t blocks = std::min<int64_t>(((int64_t)ncand + threads - 1) / threads,
                                                      (int64_t)ctx->sm_count * 16);
@@ -1631,9 +1645,11 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
             ++launches;
         }
     }
-    unsigned long long nh = 0;
-    CK(cudaMemcpyAsync(&nh, counters + 1, sizeof nh, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long cnt[4] = {0, 0, 0, 0};  // record slots, hits, -, candidates
+    CK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    const unsigned long long nh = cnt[1];
+    if (tc) ctx->stats.candidates = (int64_t)cnt[3];
     ctx->stats.hits = (int64_t)nh;
     ctx->stats.tiles = (int32_t)(tc ? ctx->tiles.size() : 0);
     ctx->stats.launches = launches;
@@ -1662,9 +1678,11 @@ int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
     if (ctx->mode != BLAMM_MODE_FP32) {
         if ((rc = ensure_plan(ctx))) return rc;
         if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(max_positions)))) return rc;
-        if (max_candidates > ctx->cand_cap) {
+        // record slots: at most one record per candidate, plus the blocks the warps reserve
+        const int64_t slots = std::min(max_candidates + record_slots_reserved(ctx->sm_count), kMaxRecordSlots);
+        if (slots > ctx->cand_cap) {
             size_t cap = ctx->cand_cap > 0 ? (size_t)ctx->cand_cap : 0;
-            rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)max_candidates);
+            rc = ensure(ctx, &ctx->d_cand, &cap, (size_t)slots);
             if (rc) return rc;
             ctx->cand_cap = (int64_t)cap;
         }
@@ -1708,12 +1726,14 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     }
     const int64_t n_mtiles = (n + kBM - 1) / kBM;
     const long long njobs = (long long)ctx->tiles.size() * n_mtiles;
+    if (int rc = check_jobs(ctx, njobs)) return rc;
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
     TcParams p = tc_params(ctx, ctx->d_e16, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
+    p.ncand = cnt + 3;
     p.cand_cap = ctx->cand_cap;
     p.status = reinterpret_cast<int *>(cnt + 2);
     p.wait_limit = ctx->wait_limit;
@@ -1721,23 +1741,8 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
     launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
     CK(cudaGetLastError());
-    RescoreParams r{};
-    r.cand = ctx->d_cand;
-    r.slot_col = ctx->d_slot_col;
-    r.cand_count = cnt;
-    r.cand_cap = ctx->cand_cap;
-    r.seq2 = ctx->d_seq2;
-    r.zmask = ctx->d_zmask;
-    r.n = n;
-    r.run_start = d_run_start;
-    r.nruns = nruns;
-    r.P = ctx->d_P;
-    r.p_rows = ctx->p_rows;
-    r.col_len = ctx->d_len;
-    r.thr = ctx->d_thr;
-    r.hits = d_hits;
-    r.hit_count = cnt + 1;
-    r.hit_cap = hit_cap;
+    const RescoreParams r = rescore_params(ctx, ctx->d_cand, cnt, ctx->cand_cap, ctx->d_seq2, ctx->d_zmask,
+                                           n, d_run_start, nruns, d_hits, cnt + 1, hit_cap);
     // a fixed grid: the candidate count is only known on the device
     rescore_kernel<<<(unsigned)(ctx->sm_count * 8), 256, 0, ctx->stream>>>(r);
     CK(cudaGetLastError());

@@ -280,11 +280,18 @@ __global__ void __launch_bounds__(256) score_hist_kernel(HistParams p)
 // ------------------------------------------------------------------------
 // 3. rescoring of tensor-core candidates: run check + exact FP32 score
 // ------------------------------------------------------------------------
+// Candidates come as 16-byte records {M tile m, row | slot << 7, mask, 0}: the position is
+// m * 128 + row, slot the first tile slot of a 32-column chunk, bit i of mask = slot + i is a
+// candidate.  The scan
+// writes them in blocks of kRecBlockSlots slots; slot 0 of a block holds the number of
+// records that follow it (the rest of the block is unused).
+constexpr int kRecBlockSlots = 128;
+
 struct RescoreParams {
-    const unsigned long long *cand;   // position << kColBits | tile slot
+    const uint4 *cand;                // record slots
     const int32_t *slot_col;          // tile slot -> motif column
-    const unsigned long long *cand_count;
-    int64_t cand_cap;
+    const unsigned long long *cand_count;  // record slots reserved
+    int64_t cand_cap;                 // record slots available
     const uint32_t *seq2;
     const uint32_t *zmask;
     int64_t n;
@@ -301,30 +308,64 @@ struct RescoreParams {
     int64_t pos_base;    // added to the positions written
 };
 
+// One thread per record slot; the candidates of a warp's 32 records are then shared out
+// over its lanes (a prefix sum of the masks' bit counts), 32 at a time, so that a record
+// with several candidates does not leave the other lanes idle.
 __global__ void __launch_bounds__(256) rescore_kernel(RescoreParams p)
 {
-    unsigned long long nc = *p.cand_count;
-    if ((int64_t)nc > p.cand_cap) nc = (unsigned long long)p.cand_cap;
+    unsigned long long ns = *p.cand_count;
+    if ((int64_t)ns > p.cand_cap) ns = (unsigned long long)p.cand_cap;
+    const int lane = threadIdx.x & 31;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < nc;
-         base += stride) {
-        unsigned long long i = base + threadIdx.x;
-        bool hit = false;
-        int64_t pos = 0;
-        int32_t col = 0;
-        float s = 0.0f;
-        if (i < nc) {
-            unsigned long long c = p.cand[i];
-            pos = (int64_t)(c >> kColBits);
-            col = __ldg(p.slot_col + (int32_t)(c & ((1u << kColBits) - 1u)));
-            const int L = __ldg(p.col_len + col);
-            if (pos + L <= run_end_of(p.run_start, p.nruns, p.n, pos)) {
-                s = window_score(p.seq2, p.zmask, p.P + (size_t)col * p.p_rows, pos, L);
-                hit = s >= __ldg(p.thr + col) && (p.keep_below == 0 || pos < p.keep_below);
-            }
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < ns; base += stride) {
+        const unsigned long long i = base + threadIdx.x;
+        uint32_t mask = 0u, mt = 0u, ry = 0u;
+        const unsigned long long b = i & ~(unsigned long long)(kRecBlockSlots - 1);
+        const uint32_t k = (uint32_t)(i & (kRecBlockSlots - 1));
+        if (i < ns && k != 0u && k <= __ldg(&p.cand[b].x)) {
+            const uint4 r = p.cand[i];
+            mt = r.x;
+            ry = r.y;
+            mask = r.z;
         }
-        emit_hits_warp(hit, pos + p.pos_base, col, s, reinterpret_cast<HitRec *>(p.hits), p.hit_count,
-                       p.hit_cap);
+        const int c = __popc(mask);
+        int incl = c;  // inclusive prefix sum of the lanes' candidate counts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            // the lane r whose record holds candidate t: the first with incl[r] > t
+            int r = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, incl, r + step - 1);
+                if (v <= t) r += step;
+            }
+            const uint32_t rmask = __shfl_sync(0xffffffffu, mask, r);
+            const uint32_t rmt = __shfl_sync(0xffffffffu, mt, r);
+            const uint32_t rry = __shfl_sync(0xffffffffu, ry, r);
+            const int before = __shfl_sync(0xffffffffu, incl, r) - __shfl_sync(0xffffffffu, c, r);
+            bool hit = false;
+            int64_t pos = 0;
+            int32_t col = 0;
+            float s = 0.0f;
+            if (t < total) {
+                const int bit = (int)__fns(rmask, 0u, t - before + 1);  // its (t - before)-th set bit
+                pos = (int64_t)rmt * 128 + (rry & 127u);
+                col = __ldg(p.slot_col + (int32_t)(rry >> 7) + bit);
+                const int L = __ldg(p.col_len + col);
+                if (pos + L <= run_end_of(p.run_start, p.nruns, p.n, pos)) {
+                    s = window_score(p.seq2, p.zmask, p.P + (size_t)col * p.p_rows, pos, L);
+                    hit = s >= __ldg(p.thr + col) && (p.keep_below == 0 || pos < p.keep_below);
+                }
+            }
+            emit_hits_warp(hit, pos + p.pos_base, col, s, reinterpret_cast<HitRec *>(p.hits), p.hit_count,
+                           p.hit_cap);
+        }
     }
 }
 

@@ -28,18 +28,27 @@
 // of sum(P), so every reference hit is a candidate; candidates are rescored
 // in exact FP32 (rescore_kernel).
 //
-// Roles (640 threads): warps 0-15 drain TMEM (lane quarter = warp % 4, column
-// group = warp / 4) and test for candidates; warps 16 and 17 (one lane each)
-// issue the MMAs of the even and the odd jobs, so that one issuer's waits,
-// commits and loop overhead overlap the other's MMAs (a thread issues about
-// one 128x256x16 MMA per 128 cycles, and a job's result reaches the drain
-// warps some 600 cycles after its last MMA); warp 18 (one lane) loads B tiles
-// and E windows with TMA bulk copies up to kEStages jobs ahead; warp 16 also
-// allocates TMEM.  kEStages E stages and 2 or 4 TMEM accumulator stages (4
-// when the plan's N tiles are at most 128 wide) keep the roles overlapped.  A
-// drain warp hands its accumulator back right after its TMEM loads; the
-// candidate test and the staging of candidates run on registers while the
-// MMAs of the next jobs proceed.  Jobs (N tile, M tile) are statically
+// Roles (640 threads, warp w on SM sub-partition w % 4): warps 0-15 drain TMEM
+// (lane quarter = warp % 4, column group = warp / 4) and test for candidates;
+// warps 16 and 17 (one lane each) issue the MMAs of the even and the odd jobs,
+// so that one issuer's waits, commits and loop overhead overlap the other's
+// MMAs (a thread issues about one 128x256x16 MMA per 128 cycles, and a job's
+// result reaches the drain warps some 600 cycles after its last MMA); their
+// waits spin instead of sleeping, since a sleeping issuer wakes late; warp 18
+// (one lane) loads B tiles and E windows with TMA bulk copies up to kEStages
+// jobs ahead; warp 16 also allocates TMEM.
+// kEStages E stages and 2 or 4 TMEM accumulator stages (4 when the plan's N
+// tiles are at most 128 wide) keep the roles overlapped.  A drain warp hands
+// its accumulator back right after its TMEM loads; a chunk holds a candidate
+// iff the maximum that the load returns is >= 0, and only then (rare) are the
+// sign masks built and one 16-byte record (M tile, row and first column slot, mask)
+// per lane with candidates written to global memory, into a block of record
+// slots the warp reserved (kRecBlock slots per atomic, the next block reserved
+// one block ahead; slot 0 of a block counts its records).  The rescoring kernel
+// expands the masks.  The drain of every job gates the next MMAs on its
+// accumulator and all 16 drain warps take part in it, so their rare path is kept
+// to registers and fire-and-forget stores: shared-memory traffic from the SIMT
+// warps queues behind the tensor cores' operand reads.  Jobs (N tile, M tile) are statically
 // interleaved over the CTAs, N-tile major, so a CTA reloads B only when its
 // tile changes: both issuers commit their old-tile MMAs to a tile-done
 // barrier, the loader then copies the new B, and both wait for it.  Every wait
@@ -57,11 +66,11 @@ namespace blamm {
 
 constexpr int kBM = 128;         // positions per M tile (= UMMA M)
 constexpr int kMaxTcLen = BLAMM_MAX_TC_MOTIF_LEN;  // longest motif on the tensor-core path
-constexpr int kCandBuf = 128;    // per-warp staging of candidates in SMEM
 constexpr int kEpiWarps = 16;    // TMEM drain warps (4 per lane quarter)
 constexpr int kMmaWarp = 16;     // issuer of the even jobs; TMEM allocation
 constexpr int kMmaWarp2 = 17;    // issuer of the odd jobs
 constexpr int kLoadWarp = 18;    // TMA bulk copies of B tiles and E windows
+constexpr int kRecBlock = kRecBlockSlots;  // candidate record slots a drain warp reserves at a time
 constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps)
 constexpr int kEStages = 6;      // E windows in flight
 constexpr int kMaxAcc = 4;       // TMEM accumulator stages (at most)
@@ -89,9 +98,10 @@ struct TcParams {
     uint32_t b_term_max; // bytes reserved per B term in SMEM
     uint32_t tmem_cols;  // TMEM columns allocated (acc_stages accumulators)
     int32_t acc_stages;  // 2 (N <= 256) or 4 (N <= 128)
-    unsigned long long *cand;
-    unsigned long long *cand_count;
-    int64_t cand_cap;
+    uint4 *cand;                      // candidate record slots: blocks of kRecBlock (see scan_tc.cuh)
+    unsigned long long *cand_count;   // record slots reserved
+    unsigned long long *ncand;        // candidates (set mask bits), added up per drain warp
+    int64_t cand_cap;                 // record slots available
     int *status;         // bit 0: a device wait timed out
     long long wait_limit;  // clock64 cycles a wait may last
     int32_t debug_stall;   // test hook: the MMA warp first waits on a barrier nobody completes
@@ -105,15 +115,20 @@ struct TcParams {
 
 // tc_prof_fields: 0/1 issuers' waits for a drained accumulator, 2 issuers' waits for B
 // tiles, 3 MMA loop, 4 loader waits for free E stages, 5 loader waits at tile changes,
-// 6 epilogue hand-back (fence + arrive), 7 epilogue wait acc_full, 8 epilogue loop,
-// 9 epilogue drain (acc_full -> acc_empty arrive), 10 jobs, 11 issuers' waits for E,
-// 12 epilogue rounds with a candidate, 13 epilogue TMEM loads, 14 epilogue fence after
-// the wait, 15 epilogue sign test and staging, 16-23 drain time of epilogue warps 0-7,
-// 24-31 their accumulator waits
+// 7 drain warp 0's accumulator waits, 8 its loop, 9 its drain (full accumulator -> hand-back),
+// 10 jobs, 11 issuers' waits for E, 12 drain warp 0's rounds with a candidate, 13 its record
+// block changes, 15 its candidate test and record writing
 
 struct TcSmem {
     // byte offsets into dynamic shared memory
-    uint32_t b_hi, b_lo, e0, abias, cand, tiles, bars, misc, total;
+    uint32_t b_hi, b_lo, e0, abias, tiles, bars, ctl, total;
+};
+
+// control words in shared memory
+enum {
+    CTL_ABORT = 0,     // set by the first wait that times out
+    CTL_TMEM = 1,      // TMEM base address
+    CTL_WORDS = 4
 };
 
 __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms, int erows, int ntiles)
@@ -130,10 +145,9 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t b_term_max, int terms,
     L.b_lo = take(terms == 2 ? b_term_max : 0, 1024);
     L.e0 = take((uint32_t)kEStages * erows * 16, 128);  // kEStages stages of erows entries
     L.abias = take(16 * 256, 128);  // 128 rows x 16 K-elements, canonical K-major layout
-    L.cand = take(kEpiWarps * kCandBuf * 8, 16);
     L.tiles = take((uint32_t)ntiles * sizeof(TileDesc), 16);
     L.bars = take(32 * 8, 8);  // BAR_COUNT <= 32
-    L.misc = take(64, 16);
+    L.ctl = take(CTL_WORDS * 4, 16);
     L.total = take(0, 1024) + 1024;  // + slack for aligning the runtime base
     return L;
 }
@@ -168,17 +182,19 @@ __device__ __forceinline__ uint32_t sign_mask(const uint32_t (&v)[32])
 
 // The jobs of one CTA: job = blockIdx.x + k * gridDim.x, tile = job / n_mtiles,
 // m = job % n_mtiles, advanced without 64-bit divisions after the first.
+// Job and M tile indices are 32-bit (the host launches at most 2^31 - 1 jobs): fewer
+// registers on the drain warps' path.
 struct JobIter {
-    long long job;
+    int job;
     int tile;
-    int64_t m;
-    __device__ __forceinline__ void init(long long j, int64_t n_mtiles)
+    int m;
+    __device__ __forceinline__ void init(int j, int n_mtiles)
     {
         job = j;
-        tile = (int)(j / n_mtiles);
-        m = j % n_mtiles;
+        tile = j / n_mtiles;
+        m = j - tile * n_mtiles;
     }
-    __device__ __forceinline__ void next(int stride, int64_t n_mtiles)
+    __device__ __forceinline__ void next(int stride, int n_mtiles)
     {
         job += stride;
         m += stride;
@@ -188,71 +204,6 @@ struct JobIter {
         }
     }
 };
-
-// Write a warp's staged candidates to the global candidate list (one atomic per warp).
-__device__ __noinline__ int flush_candidates(int lane, unsigned long long *buf, int fill, unsigned long long *cand,
-                                             unsigned long long *cand_count, int64_t cand_cap)
-{
-    __syncwarp();
-    unsigned long long gb = 0;
-    if (lane == 0 && fill > 0) gb = atomicAdd(cand_count, (unsigned long long)fill);
-    gb = __shfl_sync(0xffffffffu, gb, 0);
-    for (int i = lane; i < fill; i += 32)
-        if ((int64_t)(gb + i) < cand_cap) cand[gb + i] = buf[i];
-    __syncwarp();
-    return 0;
-}
-
-// Stage the candidates of one 32-column chunk (mask bit i = column slot0 + i of this
-// lane's position) in the warp's SMEM buffer; returns the new fill.  Warp-collective.
-// The usual case -- no lane with more than one candidate -- takes its offsets from one
-// ballot; otherwise an inclusive scan over the lanes' counts.
-__device__ __forceinline__ int stage_candidates(uint32_t mask, int slot0, int64_t pos, int lane, unsigned long long *buf,
-                                             int fill, unsigned long long *cand, unsigned long long *cand_count,
-                                             int64_t cand_cap)
-{
-    const int cnt = __popc(mask);
-    int at, total;
-    const uint32_t lt = (1u << lane) - 1u;
-    if (__ballot_sync(0xffffffffu, cnt > 1) == 0u) {
-        const uint32_t one = __ballot_sync(0xffffffffu, cnt == 1);
-        at = __popc(one & lt);
-        total = __popc(one);
-    } else {
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        total = __shfl_sync(0xffffffffu, incl, 31);
-        at = incl - cnt;
-    }
-    if (total == 0) return fill;
-    if (fill + total > kCandBuf) fill = flush_candidates(lane, buf, fill, cand, cand_count, cand_cap);
-    const unsigned long long key = (unsigned long long)pos << kColBits;
-    if (total > kCandBuf) {  // more than a buffer: straight to global memory
-        unsigned long long gb = 0;
-        if (lane == 0) gb = atomicAdd(cand_count, (unsigned long long)total);
-        gb = __shfl_sync(0xffffffffu, gb, 0);
-        while (mask) {
-            const int i = __ffs(mask) - 1;
-            mask &= mask - 1;
-            if ((int64_t)(gb + at) < cand_cap) cand[gb + at] = key | (unsigned long long)(slot0 + i);
-            ++at;
-        }
-        __syncwarp();
-        return fill;
-    }
-    while (mask) {
-        const int i = __ffs(mask) - 1;
-        mask &= mask - 1;
-        buf[fill + at] = key | (unsigned long long)(slot0 + i);
-        ++at;
-    }
-    __syncwarp();
-    return fill + total;
-}
 
 template <bool kProf>
 __device__ __forceinline__ long long tick()
@@ -273,17 +224,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     uint8_t *smem = smem_raw + ((1024 - (ptx::smem_addr(smem_raw) & 1023)) & 1023);
     const TcSmem L = tc_smem_layout(p.b_term_max, kTerms, p.erows, p.ntiles);
     const uint32_t sbase = ptx::smem_addr(smem);
-    unsigned long long *s_cand = reinterpret_cast<unsigned long long *>(smem + L.cand);
     TileDesc *s_tiles = reinterpret_cast<TileDesc *>(smem + L.tiles);
     const uint32_t bars = sbase + L.bars;
-    volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L.misc);
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(smem + L.misc + 4);
+    volatile int *ctl = reinterpret_cast<volatile int *>(smem + L.ctl);
+    volatile int *s_abort = ctl + CTL_ABORT;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // ---- set-up
     for (int i = threadIdx.x; i < p.ntiles * (int)(sizeof(TileDesc) / 4); i += blockDim.x)
         reinterpret_cast<int32_t *>(s_tiles)[i] = reinterpret_cast<const int32_t *>(p.tiles)[i];
+    for (int i = threadIdx.x; i < CTL_WORDS; i += blockDim.x)
+        if (i != CTL_TMEM) ctl[i] = 0;  // the TMEM word is written by the allocation below
     {
         // constant A of the bias MMA: every row = [1, 1, 1, 0, ...] (16 K slots)
         uint4 *ab = reinterpret_cast<uint4 *>(smem + L.abias);
@@ -293,7 +245,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         }
     }
     if (threadIdx.x == 0) {
-        *s_abort = 0;
         for (int s = 0; s < kEStages; ++s) {
             ptx::mbar_init(bars + 8 * (BAR_WFULL + s), 1);
             ptx::mbar_init(bars + 8 * (BAR_WEMPTY + s), 1);
@@ -310,17 +261,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         ptx::fence_mbar_init();
     }
     if (warp == kMmaWarp) {
-        ptx::tmem_alloc(ptx::smem_addr(s_tmem), p.tmem_cols);
+        ptx::tmem_alloc(sbase + L.ctl + 4 * CTL_TMEM, p.tmem_cols);
         ptx::tmem_relinquish();
         ptx::tc_fence_before();
     }
     ptx::fence_proxy_async_smem();  // the bias A tile is read by the tensor cores
     __syncthreads();
     ptx::tc_fence_after();
-    const uint32_t tmem_base = *s_tmem;
+    const uint32_t tmem_base = (uint32_t)ctl[CTL_TMEM];
     const uint32_t acc_stride = p.tmem_cols / (uint32_t)p.acc_stages;
     const uint32_t acc_shift = p.acc_stages == 4 ? 2u : 1u, acc_mask = (uint32_t)p.acc_stages - 1u;
-    const long long njobs = (long long)p.ntiles * p.n_mtiles;
+    const int njobs = p.ntiles * (int)p.n_mtiles;  // < 2^31 (host-checked)
+    const int n_mt = (int)p.n_mtiles;
 
     if ((warp == kMmaWarp || warp == kMmaWarp2) && lane == 0) {
         // ============ MMA issuers: warp 16 the even jobs, warp 17 the odd ones ============
@@ -338,7 +290,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         bool ok = true;
         if (p.debug_stall) ok = ptx::mbar_wait(bars + 8 * BAR_NEVER, 0, s_abort, p.wait_limit);
         JobIter it;
-        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs && ok; it.next(gridDim.x, p.n_mtiles), ++jc) {
+        for (it.init(blockIdx.x, n_mt); it.job < njobs && ok; it.next(gridDim.x, n_mt), ++jc) {
             const int tile = it.tile;
             if (tile != cur_tile) {
                 const long long tb = tick<kProf>();
@@ -360,9 +312,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             if ((jc & 1u) == mine) {
                 const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;  // accumulator
                 const long long t0 = tick<kProf>();
-                ok = ptx::mbar_wait(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
+                ok = ptx::mbar_wait_spin(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
                 const long long t1 = tick<kProf>();
-                ok = ok && ptx::mbar_wait(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
+                ok = ok && ptx::mbar_wait_spin(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
                 if (kProf) {
                     t_acc += t1 - t0;
                     t_w += tick<kProf>() - t1;
@@ -415,7 +367,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         bool b_pending = false, ok = true;
         long long t_we = 0, t_tile = 0;
         JobIter it;
-        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
+        for (it.init(blockIdx.x, n_mt); it.job < njobs; it.next(gridDim.x, n_mt), ++jc) {
             const int tile = it.tile;
             const TileDesc &td = s_tiles[tile];
             if (tile != cur_tile) {
@@ -443,7 +395,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             if (!ok) break;
             const uint32_t bytes = 16u * (uint32_t)(kBM + 4 * td.g + 2);
             ptx::mbar_arrive_expect_tx(bars + 8 * (BAR_WFULL + es), bytes);
-            ptx::bulk_g2s(sbase + L.e0 + es * (uint32_t)p.erows * 16u, p.e16 + it.m * kBM, bytes,
+            ptx::bulk_g2s(sbase + L.e0 + es * (uint32_t)p.erows * 16u, p.e16 + (int64_t)it.m * kBM, bytes,
                           bars + 8 * (BAR_WFULL + es));
             issued[es] = 1u + eph;
             if (++es == (uint32_t)kEStages) {
@@ -466,15 +418,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         // ===================== epilogue (warps 0-15) ======================
         const int q = warp & 3;     // TMEM lanes 32q .. 32q+31
         const int grp = warp >> 2;  // 32-column chunks grp, grp + 4
-        unsigned long long *buf = s_cand + warp * kCandBuf;
-        int fill = 0;
-        long long t_af = 0, t_dr = 0, n_rare = 0, t_ld = 0, t_f1 = 0, t_red = 0, t_f2 = 0;
+        const uint32_t lt = (1u << lane) - 1u;
+        // record blocks (slot indices): the current one and, in lane 0, the next one, reserved
+        // one block ahead so that the atomic's latency stays off the drain path
+        // (32-bit slot indices: the host keeps the capacity below 2^31; a block reserved
+        // beyond the capacity becomes slot index cap, whose stores are dropped)
+        const uint32_t cap = (uint32_t)p.cand_cap;
+        auto reserve = [&]() -> uint32_t {
+            const unsigned long long b = atomicAdd(p.cand_count, (unsigned long long)kRecBlock);
+            return b < (unsigned long long)cap ? (uint32_t)b : cap;
+        };
+        uint32_t blk = 0xFFFFFFFFu, nxt_blk = 0;
+        uint32_t bfill = 0;  // slots used in the current block (slot 0 is its count)
+        if (lane == 0) nxt_blk = reserve();
+        auto put = [&](uint32_t slot, uint4 v) {
+            if (slot < cap) p.cand[slot] = v;
+        };
+        auto close_block = [&]() {  // slot 0 of a block: its number of records
+            if (blk != 0xFFFFFFFFu && lane == 0) put(blk, make_uint4(bfill - 1u, 0u, 0u, 0u));
+        };
+        long long t_af = 0, t_dr = 0, n_rare = 0, t_red = 0, t_full = 0;
+        uint32_t my_cand = 0;  // this lane's candidates
         const long long t_start = tick<kProf>();
         uint32_t jc = 0;
         JobIter it;
-        for (it.init(blockIdx.x, p.n_mtiles); it.job < njobs; it.next(gridDim.x, p.n_mtiles), ++jc) {
+        for (it.init(blockIdx.x, n_mt); it.job < njobs; it.next(gridDim.x, n_mt), ++jc) {
             const int tile = it.tile;
-            const int64_t m = it.m;
+            const int m = it.m;
             const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
@@ -482,19 +452,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const long long t1 = tick<kProf>();
             if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
-            if (kProf) t_f1 += tick<kProf>() - t1;
-            const int64_t pos = m * kBM + q * 32 + lane;
-            const bool valid = pos < p.n;
+            const uint32_t row = (uint32_t)(q * 32 + lane);  // this lane's position: m * 128 + row
+            const bool valid = (int64_t)m * kBM + row < p.n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + s * acc_stride;
             // This warp's 32-column chunks grp and grp+4 (N <= 256): two TMEM loads that
             // also return each lane's maximum over the chunk, after which the accumulator
-            // is handed back at once; the candidate test on the maxima, the rare mask
-            // building and the staging all run on the registers.
+            // is handed back at once; the candidate test on the maxima and the rare mask
+            // building run on the registers.
             const int ca = grp, cb = grp + 4;
             const bool has_a = ca < nch, has_b = cb < nch;  // warp-uniform
             uint32_t va[32], vb[32];
             float max_a = -1.f, max_b = -1.f;  // each chunk's maximum, from the loads themselves
-            const long long tl0 = tick<kProf>();
             if (has_a) {
                 ptx::tmem_ld_max_32x32b_x32(taddr + ca * 32, va, max_a);
                 if (has_b) ptx::tmem_ld_max_32x32b_x32(taddr + cb * 32, vb, max_b);
@@ -503,62 +471,71 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 ptx::reg_fence(vb);
                 asm volatile("" : "+f"(max_a), "+f"(max_b));  // the same fence for the maxima
             }
-            const long long tf0 = tick<kProf>();
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(bars + 8 * (BAR_AEMPTY + s));
-            if (kProf) {
-                const long long tf1 = tick<kProf>();
-                t_ld += tf0 - tl0;
-                t_f2 += tf1 - tf0;
-                t_dr += tf1 - t1;
-            }
+            if (kProf) t_dr += tick<kProf>() - t1;
             if (has_a) {
                 const long long tr0 = tick<kProf>();
                 // maximum >= 0 <=> some column of the chunk is a candidate (a -0.0 passes
-                // here and is dropped by the sign mask, as before)
+                // here and is dropped by the sign mask)
                 const bool any_a = valid && max_a >= 0.f;
                 const bool any_b = has_b && valid && max_b >= 0.f;
-                if (__any_sync(0xffffffffu, any_a || any_b)) {  // rare: stage this warp's candidates
+                if (__any_sync(0xffffffffu, any_a || any_b)) {  // rare: publish records
                     ++n_rare;
-                    if (__any_sync(0xffffffffu, any_a))
-                        fill = stage_candidates(any_a ? sign_mask(va) : 0u, slot0 + ca * 32, pos, lane, buf, fill,
-                                                p.cand, p.cand_count, p.cand_cap);
-                    if (__any_sync(0xffffffffu, any_b))
-                        fill = stage_candidates(any_b ? sign_mask(vb) : 0u, slot0 + cb * 32, pos, lane, buf, fill,
-                                                p.cand, p.cand_count, p.cand_cap);
+                    const uint32_t ma = any_a ? sign_mask(va) : 0u, mb = any_b ? sign_mask(vb) : 0u;
+                    const uint32_t ba = __ballot_sync(0xffffffffu, ma != 0u);
+                    const uint32_t bb = __ballot_sync(0xffffffffu, mb != 0u);
+                    const uint32_t na = (uint32_t)__popc(ba), cnt = na + (uint32_t)__popc(bb);
+                    if (cnt > 0) {
+                        if (blk == 0xFFFFFFFFu || bfill + cnt > (uint32_t)kRecBlock) {  // next block
+                            const long long tw = tick<kProf>();
+                            close_block();
+                            blk = __shfl_sync(0xffffffffu, nxt_blk, 0);
+                            bfill = 1;
+                            if (lane == 0) nxt_blk = reserve();
+                            if (kProf) t_full += tick<kProf>() - tw;
+                        }
+                        // record: M tile, row | first slot of the chunk << 7, mask
+                        if (ma)
+                            put(blk + bfill + __popc(ba & lt),
+                                make_uint4((uint32_t)m, row | (uint32_t)(slot0 + ca * 32) << 7, ma, 0u));
+                        if (mb)
+                            put(blk + bfill + na + __popc(bb & lt),
+                                make_uint4((uint32_t)m, row | (uint32_t)(slot0 + cb * 32) << 7, mb, 0u));
+                        bfill += cnt;
+                        my_cand += (uint32_t)(__popc(ma) + __popc(mb));
+                    }
                 }
+                const int64_t pos = (int64_t)m * kBM + row;
                 if (kDump && pos >= p.dump_p0 && pos < p.dump_p0 + p.dump_npos) {
                     // debug instantiation only: raw accumulator of some positions
-                    float *row = p.dump + (pos - p.dump_p0) * p.dump_ncols;
+                    float *drow = p.dump + (pos - p.dump_p0) * p.dump_ncols;
 #pragma unroll
                     for (int i = 0; i < 32; ++i) {
                         int col = __ldg(p.slot_col + slot0 + ca * 32 + i);
-                        if (col >= 0) row[col] = __uint_as_float(va[i]);
+                        if (col >= 0) drow[col] = __uint_as_float(va[i]);
                         if (has_b && (col = __ldg(p.slot_col + slot0 + cb * 32 + i)) >= 0)
-                            row[col] = __uint_as_float(vb[i]);
+                            drow[col] = __uint_as_float(vb[i]);
                     }
                 }
                 if (kProf) t_red += tick<kProf>() - tr0;
             }
         }
-        fill = flush_candidates(lane, buf, fill, p.cand, p.cand_count, p.cand_cap);
-        if (kProf && lane == 0) {
+        // every reserved block states its count: the current one and the one reserved ahead
+        close_block();
+        if (lane == 0) put(nxt_blk, make_uint4(0u, 0u, 0u, 0u));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) my_cand += __shfl_xor_sync(0xffffffffu, my_cand, o);
+        if (lane == 0 && my_cand) atomicAdd(p.ncand, (unsigned long long)my_cand);
+        if (kProf && lane == 0 && warp == 0) {
             long long *pr = p.prof + 32 * blockIdx.x;
-            if (warp == 0) {
-                pr[7] = t_af;
-                pr[8] = tick<kProf>() - t_start;
-                pr[9] = t_dr;
-                pr[12] = n_rare;
-                pr[13] = t_ld;
-                pr[14] = t_f1;
-                pr[15] = t_red;
-                pr[6] = t_f2;
-            }
-            if (warp < 8) {  // counters 16..31 hold warps 0-7 only
-                pr[16 + warp] = t_dr;
-                pr[24 + warp] = t_af;
-            }
+            pr[7] = t_af;
+            pr[8] = tick<kProf>() - t_start;
+            pr[9] = t_dr;
+            pr[12] = n_rare;
+            pr[13] = t_full;
+            pr[15] = t_red;
         }
     }
 

@@ -150,10 +150,12 @@ int blamm_filter_score(blamm_ctx *ctx, float *d_R, int m, int n, const float *d_
  * blamm_scan_enqueue needs no allocation and no host synchronisation: it
  * enqueues packing, the scan and the rescoring on the context's stream and
  * returns.  counts is device memory of 4 uint64, set when the stream gets
- * there: [0] candidates, [1] hits, [2] status (non-zero: a device wait timed
- * out).  Hits beyond hit_cap and candidates beyond the reservation are counted
- * but not stored; the caller compares counts with its capacities and scans
- * again with more room.  BLAMM_ERR_STATE when the reservation or plan does not
+ * there: [0] candidate record slots used (a record holds the candidates of one
+ * position in a 32-column chunk; each CTA's warps take slots in blocks), [1]
+ * hits, [2] status (non-zero: a device wait timed out), [3] candidates.  Hits
+ * beyond hit_cap and records beyond the reservation (max_candidates plus the
+ * blocks the warps hold) are counted but not stored; the caller compares counts
+ * with its capacities and scans again with more room.  BLAMM_ERR_STATE when the reservation or plan does not
  * cover the call.
  *
  * blamm_scan_graph_create captures one blamm_scan_enqueue into an executable
@@ -259,11 +261,10 @@ int blamm_guard_band(const blamm_ctx *ctx, float *out);
  * later scans; read the last scan's counters (32 int64 per CTA, clock cycles:
  * 0 / 1 the even / odd issuer's waits for a free accumulator, 2 issuers' waits
  * for B tiles, 3 MMA loop, 4 loader waits for a free E stage, 5 loader waits at
- * tile changes, 6 epilogue hand-back, 7 epilogue waits for an accumulator,
- * 8 epilogue loop, 9 epilogue drain, 10 jobs, 11 even issuer's waits for E
- * windows, 12 epilogue rounds with candidates, 13 TMEM loads, 14 fence after the
- * wait, 15 candidate test and staging, 16-23 drain of epilogue warps 0-7, 24-31
- * their waits).  *nctas receives the
+ * tile changes, 7 drain warp 0's waits for an accumulator, 8 its loop, 9 its
+ * drain (full accumulator to hand-back), 10 jobs, 11 even issuer's waits for E
+ * windows, 12 drain warp 0's rounds with candidates, 13 its record block
+ * changes, 15 its candidate test and record writing).  *nctas receives the
  * CTA count.  The timing variant of the kernel is slower than the scan itself. */
 int blamm_debug_profile(blamm_ctx *ctx, int enable);
 /* Failure-path test hook: with enable = 1 the tensor-core scan kernel first
@@ -281,16 +282,22 @@ int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, i
  * block in the allocator).  Same arguments, results and status codes as
  * blamm_scan_device, but the packed stream, candidate list, counters and
  * status word live in one fixed array of device memory that this library
- * declares (about 73 MiB per device, reserved when the library's device code
+ * declares (about 98 MiB per device, reserved when the library's device code
  * is loaded there).  Limits: n <= 4 Mi positions per call (more gives
- * BLAMM_ERR_ARG) and at most 1 Mi tensor-core candidates per call (more gives
+ * BLAMM_ERR_ARG) and at most 2 Mi tensor-core candidate record slots per call
+ * (a record holds one position's candidates in a 32-column chunk; each CTA's
+ * warps take slots in blocks, about 0.6 Mi of them on a full GPU; more gives
  * BLAMM_ERR_OVERFLOW: scan fewer positions per call).  The counters and the
- * status word are set to zero at the start of every call.
+ * status word are set to zero at the start of every call.  Preconditions are
+ * checked before the size: an unprepared context fails the same way for an
+ * empty stream as for a non-empty one.
  * Preconditions: a bank (blamm_set_motifs) and, in the tensor-core modes, a
  * plan for the current bank, mode and thresholds, which the first
  * blamm_scan / blamm_scan_device after a change builds (otherwise
  * BLAMM_ERR_STATE).  The first call on a device looks up the array's device
- * address; make it before any stream capture.
+ * address and keeps it for the life of the process; make it before any stream
+ * capture, and do not use this entry point on a device after cudaDeviceReset
+ * (the module is reloaded and the kept address is stale).
  * The array is shared by every context on a device: calls that overlap in
  * time on one device (from two host threads, or on two streams) race on it
  * and corrupt each other's results.  Serialise them. */
