@@ -27,7 +27,8 @@ def _bg_prob(counts, pseudo=0.25):
 
 
 def test_counts_equal_the_reference_hist_files(scanner):
-    counts = [60093, 40042, 39916, 59949]  # NUCL_COUNT_ACGT of the case's dictionary
+    with open(os.path.join(GOLDEN, "expected", "sequences.mf.dict")) as f:  # the case's dictionary
+        counts = [int(x) for x in next(ln for ln in f if ln.startswith("NUCL_COUNT_ACGT")).split()[1:5]]
     bank = MotifBank.load(os.path.join(GOLDEN, "motifs.jaspar"), permutations=True, revcompl=False)
     bank.generate(np.array(counts, dtype=np.uint64), 0.25)
     P, lens, _ = bank.matrix()

@@ -83,11 +83,15 @@ def test_sequence_before_header_is_rejected(scanner):
         _gpu_parse(scanner, b"ACGT\n>s\nACGT\n")
 
 
-def test_nucleotide_counts_equal_the_reference_dictionary(scanner):
+def test_nucleotide_counts_equal_the_reference_dictionary(scanner, tmp_path):
     """The two-sequence case's sequences.mf.dict (written by the reference's dict module) holds
-    NUCL_COUNT_ACGT of its FASTA file; the GPU ingest gives the same four counts."""
+    NUCL_COUNT_ACGT of its FASTA file (stored gzip-compressed); the GPU ingest gives the same
+    four counts."""
+    import gzip
     d = os.path.join(GOLDEN, "two_sequences_1mbp")
     words = open(os.path.join(d, "expected", "sequences.mf.dict")).read().split()
     want = [int(x) for x in words[words.index("NUCL_COUNT_ACGT") + 1:][:4]]
-    got = _gpu_parse(scanner, _concat([os.path.join(d, "seqs", "seqs.fa")]))
+    fa = tmp_path / "seqs.fa"
+    fa.write_bytes(gzip.open(os.path.join(d, "seqs", "seqs.fa.gz")).read())
+    got = _gpu_parse(scanner, _concat([str(fa)]))
     assert [int(x) for x in got[5]] == want
