@@ -598,15 +598,13 @@ static int ensure_plan(blamm_ctx *ctx)
     return build_plan(ctx, terms);
 }
 
-// One-hot entries of a packed stream of n positions: the scan's E windows read up to
-// entry n + 127 + 4 * 64 + 2, and e16_kernel reads base i + 1 of the padded stream.
-static int64_t e16_entries(int64_t n) { return n + kStreamPad - 64; }
-
-static void launch_e16(const uint32_t *seq2, const uint32_t *zmask, int64_t n, uint4 *e16, cudaStream_t st)
-{
-    const int64_t ne = e16_entries(n);
-    e16_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(seq2, zmask, ne, e16);
-}
+// The tensor-core scan runs over windows of at most kEWindow positions: per window the
+// one-hot entries of its positions (e16_kernel, 16 B each) and one scan launch, so the entry
+// array holds one window (64 MB) whatever the stream length.  A window's scan reads up to
+// entry (its positions) + 127 + 4 * 64 + 2, and e16_kernel reads base i + 1 of the padded
+// stream: entries = positions + kStreamPad - 64 stay inside both.
+constexpr int64_t kEWindow = int64_t(4) << 20;
+static int64_t e16_entries(int64_t n) { return std::min(n, kEWindow) + kStreamPad - 64; }
 
 static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
 {
@@ -623,17 +621,15 @@ static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
     if (ctx->mode != BLAMM_MODE_FP32) {
         rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(n));
         if (rc) return rc;
-        launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
     }
     return BLAMM_OK;
 }
 
 // Kernel parameters of the current plan over a packed stream of n positions
 // (the caller adds candidates, counters, status and the test hooks).
-static TcParams tc_params(const blamm_ctx *ctx, const uint4 *e16, int64_t n)
+static TcParams tc_params(const blamm_ctx *ctx, int64_t n)
 {
     TcParams p{};
-    p.e16 = e16;
     p.n = n;
     p.n_mtiles = (n + kBM - 1) / kBM;
     p.tiles = ctx->d_tiles;
@@ -717,6 +713,32 @@ static void launch_tc(const TcParams &p, bool dump, int grid, uint32_t smem, cud
     else launch_tc_as<false, false>(p, grid, smem, st);
 }
 
+// The scan of n positions of a packed stream (p: the plan, candidates, counters, status),
+// window by window: the window's one-hot entries into e16, then its scan launch.  Returns the
+// largest grid used; adds the launches to *launches.
+static int launch_tc_windows(blamm_ctx *ctx, TcParams p, const uint32_t *seq2, const uint32_t *zmask, uint4 *e16,
+                             int64_t n, bool dump, uint32_t smem, int *launches, int *grid_out)
+{
+    const int64_t n_mtiles = (n + kBM - 1) / kBM, wt = kEWindow / kBM;
+    int gmax = 0;
+    for (int64_t m0 = 0; m0 < n_mtiles; m0 += wt) {
+        const int64_t mt = std::min(wt, n_mtiles - m0), base = m0 * kBM;
+        const int64_t ne = std::min(mt * kBM, n - base) + kStreamPad - 64;
+        e16_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, ctx->stream>>>(seq2, zmask, base, ne, e16);
+        CK(cudaGetLastError());
+        p.e16 = e16;
+        p.n_mtiles = mt;
+        p.m0 = (int32_t)m0;
+        const int grid = (int)std::min<long long>(ctx->sm_count, (long long)ctx->tiles.size() * mt);
+        launch_tc(p, dump, grid, smem, ctx->stream);
+        CK(cudaGetLastError());
+        gmax = std::max(gmax, grid);
+        if (launches) *launches += 2;
+    }
+    if (grid_out) *grid_out = gmax;
+    return BLAMM_OK;
+}
+
 // tcgen05 scan + rescoring; candidates buffer grows (and the scan re-runs) on overflow
 static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nruns, blamm_hit *d_hits,
                   int64_t hit_cap, float *dump, int64_t dump_p0, int64_t dump_npos, int *launches)
@@ -741,7 +763,7 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
     for (int attempt = 0; attempt < 3; ++attempt) {
         CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-        TcParams p = tc_params(ctx, ctx->d_e16, n);
+        TcParams p = tc_params(ctx, n);
         p.cand = ctx->d_cand;
         p.cand_count = ctx->d_counters;
         p.ncand = ctx->d_counters + 3;
@@ -759,13 +781,13 @@ static int run_tc(blamm_ctx *ctx, int64_t n, const int64_t *d_runs, int64_t nrun
             CK(cudaMemsetAsync(ctx->d_prof, 0, sizeof(long long) * 32 * ctx->sm_count, ctx->stream));
             p.prof = ctx->d_prof;
         }
-        const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
+        int grid = 0;
         if (njobs > 0) {
             CK(cudaEventRecord(ctx->ev[4], ctx->stream));
-            launch_tc(p, dump != nullptr, grid, smem, ctx->stream);
-            CK(cudaGetLastError());
+            if ((rc = launch_tc_windows(ctx, p, ctx->d_seq2, ctx->d_zmask, ctx->d_e16, n, dump != nullptr, smem,
+                                        launches, &grid)))
+                return rc;
             CK(cudaEventRecord(ctx->ev[5], ctx->stream));
-            ++*launches;
         }
         unsigned long long ncand = 0;
         int status = 0;
@@ -886,7 +908,7 @@ static int scan_core(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     int rc = launch_pack(ctx, d_bases, n);
     if (rc) return rc;
-    launches += ctx->mode == BLAMM_MODE_FP32 ? 1 : 2;  // packing (+ one-hot entries)
+    launches += 1;  // packing (the tensor-core scan adds its windows' one-hot entries)
     if (ctx->mode == BLAMM_MODE_FP32) rc = run_plain(ctx, n, d_runs, nruns, d_hits, hit_cap, &launches);
     else rc = run_tc(ctx, n, d_runs, nruns, d_hits, hit_cap, nullptr, 0, 0, &launches);
     if (rc) return rc;
@@ -1032,8 +1054,6 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
         PlainParams p = plain_params(ctx, ctx->d_seq2, ctx->d_zmask, n, d_runs, nruns, d_hits, hit_cap, cnt + 1);
         return launch_plain(ctx, p);
     }
-    launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
-    CK(cudaGetLastError());
     CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));      // record slots of this chunk
     CK(cudaMemsetAsync(cnt + 3, 0, sizeof(unsigned long long), ctx->stream));  // its candidates
     const int64_t n_mtiles = (n + kBM - 1) / kBM;
@@ -1043,7 +1063,7 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
-    TcParams p = tc_params(ctx, ctx->d_e16, n);
+    TcParams p = tc_params(ctx, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
     p.ncand = cnt + 3;
@@ -1051,9 +1071,9 @@ static int enqueue_chunk(blamm_ctx *ctx, const char *d_bases, int64_t n, const i
     p.status = ctx->d_status;
     p.wait_limit = ctx->wait_limit;
     p.dump_ncols = ctx->ncols;
-    const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-    launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
-    CK(cudaGetLastError());
+    if ((rc = launch_tc_windows(ctx, p, ctx->d_seq2, ctx->d_zmask, ctx->d_e16, n, false,
+                                std::max<uint32_t>(L.total, 116 * 1024), nullptr, nullptr)))
+        return rc;
     const RescoreParams r = rescore_params(ctx, ctx->d_cand, cnt, ctx->cand_cap, ctx->d_seq2, ctx->d_zmask,
                                            n, d_runs, nruns, d_hits, cnt + 1, hit_cap);
     rescore_kernel<<<(unsigned)(ctx->sm_count * 8), 256, 0, ctx->stream>>>(r);
@@ -1188,7 +1208,11 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
     total.positions = n;
     total.columns = scanned_columns(ctx);
     total.tiles = (int32_t)(tc ? ctx->tiles.size() : 0);
-    total.launches = (int32_t)(nchunks * (tc ? 4 : 2));
+    total.launches = 0;
+    for (int64_t k = 0; k < nchunks; ++k) {  // packing + scan (+ rescoring and a one-hot build per window)
+        const int64_t len = std::min(n, (k + 1) * kPipeChunk + ov) - k * kPipeChunk;
+        total.launches += (int32_t)(tc ? 2 + 2 * ((len + kEWindow - 1) / kEWindow) : 2);
+    }
     int status = 0;
     for (int64_t k = 0; k < nchunks; ++k) {
         const int64_t nc = (int64_t)hc_k[4 * k];
@@ -1595,11 +1619,6 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
                                                                           ctx->lower_scores);
     CK(cudaGetLastError());
     ++launches;
-    if (tc) {
-        launch_e16(seq2, zmask, n, e16, ctx->stream);
-        CK(cudaGetLastError());
-        ++launches;
-    }
 
     if (!tc) {
         PlainParams p = plain_params(ctx, seq2, zmask, n, d_run_start, nruns, d_hits, hit_cap, counters + 1);
@@ -1612,7 +1631,7 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         if ((int)L.total > ctx->max_smem)
             return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
         const uint32_t smem = std::max<uint32_t>(L.total, 116 * 1024);
-        TcParams p = tc_params(ctx, e16, n);
+        TcParams p = tc_params(ctx, n);
         p.cand = cand;
         p.cand_count = counters;
         p.ncand = counters + 3;
@@ -1620,10 +1639,8 @@ int blamm_scan_device_static(blamm_ctx *ctx, const char *d_bases, int64_t n, con
         p.status = status;
         p.wait_limit = ctx->wait_limit;
         p.dump_ncols = ctx->ncols;
-        const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-        launch_tc(p, false, grid, smem, ctx->stream);
-        CK(cudaGetLastError());
-        ++launches;
+        (void)njobs;
+        if ((rc = launch_tc_windows(ctx, p, seq2, zmask, e16, n, false, smem, &launches, nullptr))) return rc;
         unsigned long long ncand = 0;
         int st = 0;
         CK(cudaMemcpyAsync(&ncand, counters, sizeof ncand, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1716,10 +1733,6 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     pack_kernel<<<(unsigned)((nwords32 + 255) / 256), 256, 0, ctx->stream>>>(d_bases, n, ctx->d_seq2, ctx->d_zmask,
                                                                           nwords32, ctx->lower_scores);
     CK(cudaGetLastError());
-    if (tc) {
-        launch_e16(ctx->d_seq2, ctx->d_zmask, n, ctx->d_e16, ctx->stream);
-        CK(cudaGetLastError());
-    }
     if (!tc) {
         PlainParams p = plain_params(ctx, ctx->d_seq2, ctx->d_zmask, n, d_run_start, nruns, d_hits, hit_cap, cnt + 1);
         return launch_plain(ctx, p);
@@ -1730,7 +1743,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     const TcSmem L = tc_smem_layout(ctx->b_term_max, ctx->plan_terms, ctx->erows, (int)ctx->tiles.size());
     if ((int)L.total > ctx->max_smem)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "shared memory plan %u > %d", L.total, ctx->max_smem);
-    TcParams p = tc_params(ctx, ctx->d_e16, n);
+    TcParams p = tc_params(ctx, n);
     p.cand = ctx->d_cand;
     p.cand_count = cnt;
     p.ncand = cnt + 3;
@@ -1738,9 +1751,9 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     p.status = reinterpret_cast<int *>(cnt + 2);
     p.wait_limit = ctx->wait_limit;
     p.dump_ncols = ctx->ncols;
-    const int grid = (int)std::min<long long>(ctx->sm_count, std::max<long long>(njobs, 1));
-    launch_tc(p, false, grid, std::max<uint32_t>(L.total, 116 * 1024), ctx->stream);
-    CK(cudaGetLastError());
+    if (int rc = launch_tc_windows(ctx, p, ctx->d_seq2, ctx->d_zmask, ctx->d_e16, n, false,
+                                   std::max<uint32_t>(L.total, 116 * 1024), nullptr, nullptr))
+        return rc;
     const RescoreParams r = rescore_params(ctx, ctx->d_cand, cnt, ctx->cand_cap, ctx->d_seq2, ctx->d_zmask,
                                            n, d_run_start, nruns, d_hits, cnt + 1, hit_cap);
     // a fixed grid: the candidate count is only known on the device

@@ -105,15 +105,16 @@ __device__ __forceinline__ uint2 onehot_bf16(uint32_t code, uint32_t zero)
     return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
 }
 
-__global__ void e16_kernel(const uint32_t *__restrict__ seq2, const uint32_t *__restrict__ zmask, int64_t ne,
-                           uint4 *__restrict__ e16)
+// Entries of one window of the stream: e16[i] = entry of position base + i, i < ne.
+__global__ void e16_kernel(const uint32_t *__restrict__ seq2, const uint32_t *__restrict__ zmask, int64_t base,
+                           int64_t ne, uint4 *__restrict__ e16)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ne) return;
-    const int64_t j = i + 1;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ne) return;
+    const int64_t i = base + t, j = i + 1;
     const uint2 a = onehot_bf16((seq2[i >> 4] >> (2 * (i & 15))) & 3u, (zmask[i >> 5] >> (i & 31)) & 1u);
     const uint2 b = onehot_bf16((seq2[j >> 4] >> (2 * (j & 15))) & 3u, (zmask[j >> 5] >> (j & 31)) & 1u);
-    e16[i] = make_uint4(a.x, a.y, b.x, b.y);
+    e16[t] = make_uint4(a.x, a.y, b.x, b.y);
 }
 
 // ------------------------------------------------------------------------

@@ -2,7 +2,9 @@
 // one persistent CTA per SM.
 //
 // Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
-// After packing, e16_kernel writes one 16-byte entry per stream position,
+// After packing, e16_kernel writes one 16-byte entry per stream position of a
+// window of at most 4 Mi positions (the scan runs once per window, so the entry
+// array stays 64 MB whatever the stream length),
 // E[i] = onehot(base i) ++ onehot(base i+1) (2 bases x 4 channels x bf16).
 // For an M tile of 128 positions starting at m0, a bulk copy brings entries
 // m0 .. m0+128+4g+1 into shared memory; read with row stride 16 B, 8-row group
@@ -86,9 +88,10 @@ struct TileDesc {
 };
 
 struct TcParams {
-    const uint4 *e16;    // one-hot entries of the stream (16 B per position, padded)
+    const uint4 *e16;    // one-hot entries of this launch's window (16 B per position, padded)
     int64_t n;           // stream positions
-    int64_t n_mtiles;    // ceil(n / 128)
+    int64_t n_mtiles;    // M tiles of this launch's window
+    int32_t m0;          // the window's first M tile in the stream
     const TileDesc *tiles;
     int32_t ntiles;
     int32_t terms;       // 1 (hi) or 2 (hi + lo)
@@ -350,12 +353,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         if (!ptx::mbar_wait_drain(bars + 8 * (BAR_DRAIN + mine), 0, p.wait_limit)) *s_abort = 1;
         if (kProf) {
             long long *pr = p.prof + 32 * blockIdx.x;
-            pr[mine] = t_acc;
+            pr[mine] += t_acc;
             if (mine == 0) {
-                pr[2] = t_b;
-                pr[3] = tick<kProf>() - t_start;
-                pr[10] = jc;
-                pr[11] = t_w;
+                pr[2] += t_b;
+                pr[3] += tick<kProf>() - t_start;
+                pr[10] += jc;
+                pr[11] += t_w;
             }
         }
     } else if (warp == kLoadWarp && lane == 0) {
@@ -411,8 +414,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         }
         if (kProf) {
             long long *pr = p.prof + 32 * blockIdx.x;
-            pr[4] = t_we;
-            pr[5] = t_tile;
+            pr[4] += t_we;
+            pr[5] += t_tile;
         }
     } else if (warp < kEpiWarps) {
         // ===================== epilogue (warps 0-15) ======================
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         JobIter it;
         for (it.init(blockIdx.x, n_mt); it.job < njobs; it.next(gridDim.x, n_mt), ++jc) {
             const int tile = it.tile;
-            const int m = it.m;
+            const int m = p.m0 + it.m;  // M tile in the stream
             const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
@@ -530,12 +533,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         if (lane == 0 && my_cand) atomicAdd(p.ncand, (unsigned long long)my_cand);
         if (kProf && lane == 0 && warp == 0) {
             long long *pr = p.prof + 32 * blockIdx.x;
-            pr[7] = t_af;
-            pr[8] = tick<kProf>() - t_start;
-            pr[9] = t_dr;
-            pr[12] = n_rare;
-            pr[13] = t_full;
-            pr[15] = t_red;
+            pr[7] += t_af;
+            pr[8] += tick<kProf>() - t_start;
+            pr[9] += t_dr;
+            pr[12] += n_rare;
+            pr[13] += t_full;
+            pr[15] += t_red;
         }
     }
 
