@@ -1546,7 +1546,7 @@ constexpr size_t kStaticE16Off = round256(kStaticZmaskOff + sizeof(uint32_t) * k
 constexpr size_t kStaticCandOff = round256(kStaticE16Off + sizeof(uint4) * (kStaticMaxBases + kStreamPad));
 constexpr size_t kStaticCountOff = round256(kStaticCandOff + sizeof(uint4) * kStaticCandCap);
 constexpr size_t kStaticStatusOff = round256(kStaticCountOff + sizeof(unsigned long long) * 4);
-constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 73 MiB
+constexpr size_t kStaticBytes = round256(kStaticStatusOff + sizeof(int));  // about 97 MiB
 
 constexpr int kStaticMaxDevices = 64;
 

@@ -282,7 +282,7 @@ int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, i
  * block in the allocator).  Same arguments, results and status codes as
  * blamm_scan_device, but the packed stream, candidate list, counters and
  * status word live in one fixed array of device memory that this library
- * declares (about 98 MiB per device, reserved when the library's device code
+ * declares (about 97 MiB per device, reserved when the library's device code
  * is loaded there).  Limits: n <= 4 Mi positions per call (more gives
  * BLAMM_ERR_ARG) and at most 2 Mi tensor-core candidate record slots per call
  * (a record holds one position's candidates in a 32-column chunk; each CTA's

@@ -70,3 +70,64 @@ def test_static_rejects_oversize_and_missing_plan():
         assert "static limit" in str(e.value)
     finally:
         sc.close()
+
+
+def test_static_at_the_position_limit_matches_scan_device():
+    """n equal to the fixed scratch's limit (the offsets of its regions are sized for it)."""
+    torch = pytest.importorskip("torch")
+    n = STATIC_MAX_BASES
+    P, lens, thr = make_bank(21, 12, 5, 30, rel=0.93)
+    bases, runs = make_stream(22, n, nruns=9, lower_frac=0.01)
+    d_b = torch.from_numpy(bases).cuda()
+    d_r = torch.from_numpy(runs).cuda()
+    sc = GpuScanner(0, "bf16")
+    try:
+        sc.set_motifs(P, lens, thr)
+        cap = 2 << 20
+        d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+        want = _hits(torch, d_h, nh)
+        assert nh > 100
+        d_h.zero_()
+        got_n = sc.scan_device_static(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+        ok, msg = same_hits(_hits(torch, d_h, got_n), want)
+        assert ok, msg
+    finally:
+        sc.close()
+
+
+def test_static_overflow_returns():
+    """More candidate records than the fixed scratch holds, and more hits than the caller's
+    buffer: both end in BLAMM_ERR_OVERFLOW; the context then scans normally again."""
+    torch = pytest.importorskip("torch")
+    from blamm_gb300._native import BLAMM_ERR_OVERFLOW
+    n = 3_000_000
+    P, lens, thr = make_bank(23, 48, 5, 12, rel=0.3)  # most windows pass: ~n x 3 records
+    bases, runs = make_stream(24, n, nruns=5)
+    d_b = torch.from_numpy(bases).cuda()
+    d_r = torch.from_numpy(runs).cuda()
+    sc = GpuScanner(0, "bf16")
+    try:
+        sc.set_motifs(P, lens, thr)
+        cap = 1 << 16
+        d_h = torch.empty(cap * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        sc.scan_device(d_b.data_ptr(), 4096, d_r.data_ptr(), 1, d_h.data_ptr(), cap, overflow_ok=True)  # plan
+        with pytest.raises(BlammError) as e:
+            sc.scan_device_static(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), d_h.data_ptr(), cap)
+        assert e.value.code == BLAMM_ERR_OVERFLOW and "static limit" in str(e.value)
+        # hits beyond the caller's capacity (a stream short enough for the records)
+        m = 40_000
+        with pytest.raises(BlammError) as e:
+            sc.scan_device_static(d_b.data_ptr(), m, d_r.data_ptr(), 1, d_h.data_ptr(), 16)
+        assert e.value.code == BLAMM_ERR_OVERFLOW
+        # the context and the scratch are still good
+        P2, l2, t2 = make_bank(25, 24, 5, 20, rel=0.9)
+        sc.set_motifs(P2, l2, t2)
+        nh = sc.scan_device(d_b.data_ptr(), m, d_r.data_ptr(), 1, d_h.data_ptr(), cap)
+        want = _hits(torch, d_h, nh)
+        d_h.zero_()
+        got = sc.scan_device_static(d_b.data_ptr(), m, d_r.data_ptr(), 1, d_h.data_ptr(), cap)
+        ok, msg = same_hits(_hits(torch, d_h, got), want)
+        assert ok, msg
+    finally:
+        sc.close()
