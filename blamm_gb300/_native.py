@@ -94,6 +94,8 @@ def gpu_lib() -> C.CDLL:
                                              C.POINTER(i64), vp]
     lib.blamm_get_plan_options.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     lib.blamm_get_terms.argtypes = [vp]
+    lib.blamm_ctx_call_bytes.argtypes = [vp, C.POINTER(i64)]
+    lib.blamm_release_buffers.argtypes = [vp]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
@@ -101,7 +103,8 @@ def gpu_lib() -> C.CDLL:
                  "blamm_debug_profile_read", "blamm_scan_device_static", "blamm_set_columns",
                  "blamm_reserve", "blamm_scan_enqueue", "blamm_scan_graph_create", "blamm_scan_graph_launch",
                  "blamm_autotune", "blamm_theoretical_hist", "blamm_device_memory", "blamm_set_plan_options",
-                 "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall", "blamm_get_terms"):
+                 "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall", "blamm_get_terms",
+                 "blamm_ctx_call_bytes", "blamm_release_buffers"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -272,6 +275,15 @@ class GpuScanner:
         self._check(self.lib.blamm_get_plan_options(self.h, C.byref(n), C.byref(c)))
         return n.value, c.value
 
+    def call_bytes(self) -> int:
+        """Device bytes of the per-call buffers the context keeps."""
+        b = C.c_int64(0)
+        self._check(self.lib.blamm_ctx_call_bytes(self.h, C.byref(b)))
+        return b.value
+
+    def release_buffers(self) -> None:
+        self._check(self.lib.blamm_release_buffers(self.h))
+
     def terms(self) -> int:
         """BF16 terms of the tensor-core scan in the current mode (0 in FP32 mode)."""
         return int(self.lib.blamm_get_terms(self.h))
@@ -408,7 +420,8 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
                 ("queued", C.c_int64), ("bases", C.c_int64), ("bp_columns", C.c_double),
-                ("bytes_in_flight", C.c_int64), ("budget", C.c_int64)]
+                ("bytes_in_flight", C.c_int64), ("bytes_held", C.c_int64), ("peak_committed", C.c_int64),
+                ("budget", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -1,4 +1,5 @@
-"""Builds the native parts of blamm_gb300 in-tree.
+"""Builds the native parts of blamm_gb300 in-tree (the test infrastructure -- the CPU oracle
+and the reference binary -- has its own build, oracle/oracle_build.py).
 
   libblamm_gpu.so   CUDA kernels + the C ABI of include/blamm_gpu.h (sm_103a only)
   libblamm_host.so  C++ host library of include/blamm_host.h (motifs, PWMs,
@@ -92,21 +93,8 @@ def _host(force: bool, pool: ThreadPoolExecutor) -> tuple[str, str]:
     return lib, exe
 
 
-def _oracle(force: bool) -> None:
-    odir = os.path.join(ROOT, "oracle")
-    args = ["make", "-s", "-C", odir]
-    if force:
-        _run(["make", "-s", "-C", odir, "clean"])
-    _run(args)
-
-
-def build(force: bool = False, with_reference: bool = True) -> None:
-    """Compile every native part (GPU library, host library, CLI, CPU oracle).
-
-    The reference binary (test infrastructure) is compiled too when its
-    sources are mounted at /root/reference, which is only the case in the
-    development container; GPU machines use the committed fixtures instead.
-    """
+def build(force: bool = False) -> None:
+    """Compile every native part of the product (GPU library, host library, CLI)."""
     os.makedirs(BUILD, exist_ok=True)
     # objects of another architecture (a copy built on x86 arriving on an Arm box) are rebuilt
     stamp = os.path.join(BUILD, ".arch")
@@ -114,18 +102,11 @@ def build(force: bool = False, with_reference: bool = True) -> None:
     if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
         force = True
     with ThreadPoolExecutor(max_workers=8) as pool:
-        f_gpu = pool.submit(_gpu_lib, force)
-        f_orc = pool.submit(_oracle, force)
-        f_gpu.result()  # the CLI links the GPU library
+        _gpu_lib(force)  # the CLI links the GPU library
         if all(os.path.exists(os.path.join(CSRC, "host", s)) for s in HOST_SRCS + ["blamm_main.cpp"]):
             _host(force, pool)
-        f_orc.result()
     with open(stamp, "w") as f:
         f.write(arch + "\n")
-    ref_src = "/root/reference/src"
-    ref_bin = os.path.join(ROOT, "oracle", "_ref", "blamm")
-    if with_reference and os.path.isdir(ref_src) and (force or not os.path.exists(ref_bin)):
-        _run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
 
 
 if __name__ == "__main__":

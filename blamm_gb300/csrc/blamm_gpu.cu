@@ -488,6 +488,56 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
     delete ctx;
 }
 
+// Device bytes of the per-call buffers (stream, packed stream, one-hot window, run table,
+// candidate records, hits, pipeline chunks); the motif bank and its plan are not counted.
+static int64_t call_buffer_bytes(const blamm_ctx *ctx)
+{
+    return (int64_t)(ctx->cap_bases + 4 * ctx->cap_words32 + 4 * ctx->cap_zmask + 16 * ctx->cap_e16 +
+                     8 * ctx->cap_runs + 8 * (ctx->cap_chunk_runs[0] + ctx->cap_chunk_runs[1]) +
+                     ctx->cap_chunk_bases[0] + ctx->cap_chunk_bases[1]) +
+           16 * ctx->cand_cap + (int64_t)sizeof(blamm_hit) * ctx->hits_cap;
+}
+
+int blamm_ctx_call_bytes(const blamm_ctx *ctx, int64_t *bytes)
+{
+    if (!ctx || !bytes) return BLAMM_ERR_ARG;
+    *bytes = call_buffer_bytes(ctx);
+    return BLAMM_OK;
+}
+
+int blamm_release_buffers(blamm_ctx *ctx)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->copy_stream) CK(cudaStreamSynchronize(ctx->copy_stream));
+    auto drop = [&](auto **ptr, auto *cap) {
+        if (*ptr) cudaFreeAsync(*ptr, ctx->stream);
+        *ptr = nullptr;
+        *cap = 0;
+    };
+    drop(&ctx->d_bases, &ctx->cap_bases);
+    drop(&ctx->d_seq2, &ctx->cap_words32);
+    drop(&ctx->d_zmask, &ctx->cap_zmask);
+    drop(&ctx->d_e16, &ctx->cap_e16);
+    drop(&ctx->d_runs, &ctx->cap_runs);
+    for (int b = 0; b < 2; ++b) {
+        drop(&ctx->d_chunk_bases[b], &ctx->cap_chunk_bases[b]);
+        drop(&ctx->d_chunk_runs[b], &ctx->cap_chunk_runs[b]);
+    }
+    if (ctx->d_cand) cudaFreeAsync(ctx->d_cand, ctx->stream);
+    ctx->d_cand = nullptr;
+    ctx->cand_cap = 0;
+    if (ctx->d_hits) cudaFreeAsync(ctx->d_hits, ctx->stream);
+    ctx->d_hits = nullptr;
+    ctx->hits_cap = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    // give the freed memory back to the device: the stream-ordered pool would keep it
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    return BLAMM_OK;
+}
+
 const char *blamm_last_error(const blamm_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 int blamm_set_mode(blamm_ctx *ctx, int mode)

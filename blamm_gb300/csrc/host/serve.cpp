@@ -3,7 +3,10 @@
 // One GPU context per slot (its own CUDA stream and device buffers), one host
 // thread per slot.  Slot threads take requests from a FIFO queue as soon as
 // they are free and the request's device-memory estimate fits the budget left
-// by the requests in flight; a request runs as blamm_set_thresholds (when its
+// by the requests in flight and the buffers the slots' contexts keep from earlier
+// requests (measured after each request); when the queue's head cannot fit and
+// nothing is in flight, every slot releases its kept buffers.  A request runs as
+// blamm_set_thresholds (when its
 // set differs from the slot's) + blamm_set_columns + blamm_scan on its slot.
 // Work of different slots overlaps on the device: host<->device copies of one
 // request run beside the kernels of another, and a small request's persistent
@@ -45,6 +48,7 @@ struct Request {
 struct Slot {
     blamm_ctx *ctx = nullptr;
     int set = -1;
+    int64_t held = 0;  // device bytes the context keeps between requests
     std::thread th;
 };
 
@@ -62,6 +66,8 @@ struct blamm_server {
     std::unordered_map<int64_t, std::shared_ptr<Request>> reqs;
     int64_t next_id = 1;
     int64_t in_flight_bytes = 0;
+    int64_t held_bytes = 0;  // sum of the slots' held bytes
+    bool release = false;    // the queue's head waits for the slots' kept buffers
     int64_t budget = 0;
     bool stop = false;
     blamm_server_stats st{};
@@ -84,13 +90,15 @@ int fail(blamm_server *s, int code, const char *fmt, ...)
     return code;
 }
 
-// Device bytes a request holds while it runs: raw and packed stream, its one-hot
-// entries (16 B per position), run table, candidates (at least the context's initial
-// 1 Mi list), hits, tile plan.
+// Device bytes a request holds while it runs: raw and packed stream, the one-hot entries
+// of one scan window (16 B per position, at most 4 Mi positions), run table, candidate
+// records (16 B; at least the context's initial 1 Mi, plus the blocks the scan's warps
+// reserve), hits, tile plan.
 int64_t request_bytes(int64_t n, int64_t nruns, int64_t cols, int p_rows)
 {
-    const int64_t stream = n + (n + 2048) / 32 * 12 + 16 * (n + 2048) + 8 * nruns;
-    const int64_t cand = 8 * std::max<int64_t>(int64_t(1) << 20, n * cols / 1000);
+    const int64_t stream =
+        n + (n + 2048) / 32 * 12 + 16 * (std::min<int64_t>(n, int64_t(4) << 20) + 2048) + 8 * nruns;
+    const int64_t cand = 16 * std::max<int64_t>(int64_t(1) << 20, n * cols / 1000 + 152 * 16 * 2 * 128);
     const int64_t hits = 16 * std::max<int64_t>(int64_t(1) << 16, n * cols / 2000);
     const int64_t plan = cols * (int64_t)p_rows * 2 * 2 * 2 + (int64_t(1) << 20);
     return stream + cand + hits + plan;
@@ -139,24 +147,55 @@ void slot_loop(blamm_server *s, int k)
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait(lk, [&] {
                 if (s->stop) return true;
+                if (s->release && slot.held > 0) return true;  // give the kept buffers back
                 if (s->queue.empty()) return false;
-                // first in, first out: the head is admitted when it fits beside the requests in flight
+                // first in, first out: the head is admitted when it fits beside the requests in
+                // flight and the buffers the other slots keep (this slot's are reused by it)
                 const int64_t need = s->queue.front()->need;
-                return s->in_flight_bytes == 0 || s->in_flight_bytes + need <= s->budget;
+                if (s->in_flight_bytes + s->held_bytes - slot.held + need <= s->budget) return true;
+                if (s->in_flight_bytes == 0 && !s->release) {
+                    s->release = true;  // nothing runs: the slots release what they keep
+                    s->cv_work.notify_all();
+                }
+                return s->in_flight_bytes == 0 && s->held_bytes == slot.held;  // every other slot released
             });
             if (s->stop) return;
+            if (s->release && slot.held > 0 && s->in_flight_bytes + s->held_bytes - slot.held +
+                                                       (s->queue.empty() ? 0 : s->queue.front()->need) > s->budget) {
+                const int64_t had = slot.held;
+                lk.unlock();
+                blamm_release_buffers(slot.ctx);
+                int64_t now = 0;
+                blamm_ctx_call_bytes(slot.ctx, &now);
+                lk.lock();
+                slot.held = now;
+                s->held_bytes += now - had;
+                if (s->held_bytes == 0 || s->in_flight_bytes > 0) s->release = false;
+                s->cv_work.notify_all();
+                continue;
+            }
+            if (s->queue.empty()) continue;
+            s->release = false;
             r = s->queue.front();
             s->queue.pop_front();
             s->in_flight_bytes += r->need;
+            // committed: the requests in flight plus the other slots' kept buffers
+            s->st.peak_committed =
+                std::max(s->st.peak_committed, s->in_flight_bytes + s->held_bytes - slot.held);
             r->t_admit = Clock::now();
         }
         s->cv_work.notify_all();  // the next request may fit too
         run_request(s, slot, *r);
+        int64_t kept = 0;
+        blamm_ctx_call_bytes(slot.ctx, &kept);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             r->t_done = Clock::now();
             r->done = true;
             s->in_flight_bytes -= r->need;
+            s->held_bytes += kept - slot.held;
+            slot.held = kept;
+            s->st.peak_committed = std::max(s->st.peak_committed, s->in_flight_bytes + s->held_bytes);
             if (r->status == BLAMM_OK) {
                 s->st.completed += 1;
                 s->st.bases += (int64_t)r->bases.size();
@@ -291,6 +330,7 @@ int blamm_server_stats_get(blamm_server *s, blamm_server_stats *out)
     *out = s->st;
     out->queued = (int64_t)s->queue.size();
     out->bytes_in_flight = s->in_flight_bytes;
+    out->bytes_held = s->held_bytes;
     out->budget = s->budget;
     return BLAMM_OK;
 }

@@ -276,6 +276,14 @@ int blamm_debug_profile(blamm_ctx *ctx, int enable);
 int blamm_debug_stall(blamm_ctx *ctx, int enable, long long wait_limit_cycles);
 int blamm_debug_profile_read(const blamm_ctx *ctx, int64_t *out, int max_ctas, int *nctas);
 
+/* Device memory held for scans (no counterpart in the reference, whose threads allocate
+ * per run): a context keeps the per-call buffers of its largest scan so far (stream, packed
+ * stream, one-hot window, run table, candidate records, hits).  blamm_ctx_call_bytes reports
+ * their size; blamm_release_buffers frees them (the motif bank and its plan stay) after the
+ * context's stream has drained, and trims the device's stream-ordered memory pool. */
+int blamm_ctx_call_bytes(const blamm_ctx *ctx, int64_t *bytes);
+int blamm_release_buffers(blamm_ctx *ctx);
+
 /* blamm_scan_device without allocation.  It has no counterpart in the
  * reference; it is for callers that may not allocate device or host memory
  * during a scan (a memory pool that must not grow, a host thread that must not

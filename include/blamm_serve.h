@@ -15,11 +15,14 @@
  *     (a small request occupies only the SMs its jobs need);
  *   - admission by device memory: a request is admitted when the device bytes
  *     it needs (stream, packed stream, candidates, hits, tile plan; an estimate
- *     made at submission) fit in what the requests in flight leave of the
- *     budget.  Admission is first in, first out.  A slot's context keeps the
- *     device buffers of the largest request it has run (they are reused, not
- *     freed), and the budget counts requests in flight only: with requests
- *     near the budget, set hbm_budget to the free memory divided by the slots;
+ *     made at submission) fit in what the requests in flight and the buffers the
+ *     slots keep leave of the budget.  Admission is first in, first out.  A
+ *     slot's context keeps the device buffers of the largest request it has run
+ *     (they are reused: the slot's own kept bytes count toward its next request);
+ *     their size is measured after every request.  When the queue's head does
+ *     not fit and nothing is in flight, every slot releases its kept buffers
+ *     (blamm_release_buffers), so a request that fits the budget alone always
+ *     runs;
  *   - results: the hits of a request are the same alone and in any mix (each
  *     request has its own context; scores are exact FP32, see blamm_gpu.h).
  *
@@ -51,6 +54,8 @@ typedef struct {
     int64_t bases;            /* positions scanned by completed requests */
     double bp_columns;        /* sum over completed requests of positions x columns */
     int64_t bytes_in_flight;  /* admitted estimate */
+    int64_t bytes_held;       /* device bytes the slots' contexts keep between requests */
+    int64_t peak_committed;   /* largest in-flight estimate + kept bytes seen at admission or completion */
     int64_t budget;
 } blamm_server_stats;
 

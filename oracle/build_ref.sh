@@ -5,12 +5,14 @@
 # the binary is the checker that pins the oracle restatement and generates the
 # golden fixtures; nothing in the product links or runs it.
 #
-#   usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+#   usage: oracle/build_ref.sh [reference_root]
+#   (default: $BLAMM_REFERENCE_DIR, else the DEFAULT_REF below)
 #
 # BLAS: scipy's bundled LP64 OpenBLAS (exports scipy_sgemm_).  numpy's
 # scipy_openblas64_ is ILP64 and must not be used (wrong integer width).
 set -euo pipefail
-REF=${1:-/root/reference}
+DEFAULT_REF=/root/reference
+REF=${1:-${BLAMM_REFERENCE_DIR:-$DEFAULT_REF}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 2; }

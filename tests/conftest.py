@@ -19,6 +19,8 @@ def _built():
     """Compile (or re-use) every native part once per session."""
     from blamm_gb300 import build
     build.build()
+    import oracle_build  # oracle/oracle_build.py (oracle/ is on sys.path)
+    oracle_build.build()
     yield
 
 

@@ -181,32 +181,29 @@ def test_genome_parts_share_the_bank_and_not_the_bases():
     assert not np.array_equal(a.sequences[0][1][:1000], b.sequences[0][1][:1000])
 
 
-REFERENCE_SRC = "/root/reference/src"
 CUDA_INCLUDE = "/usr/local/cuda/include"
 
 
 def test_integration_stub_compiles_against_the_reference(tmp_path):
-    """The replacement body of PWMScan::scanThreadCUBLAS in INTEGRATION.md compiles (syntax
-    and types) against the reference's unmodified headers and include/blamm_gpu.h."""
+    """The replacement body of PWMScan::scanThreadCUBLAS (tests/integration_stub.cpp) compiles
+    (syntax and types) against the reference's unmodified headers and include/blamm_gpu.h."""
     import shutil
     import subprocess
-    if not os.path.isdir(REFERENCE_SRC) or not os.path.isdir(CUDA_INCLUDE) or not shutil.which("g++"):
+    import oracle_build
+    ref_src = os.path.join(oracle_build.reference_dir(), "src")
+    if not os.path.isdir(ref_src) or not os.path.isdir(CUDA_INCLUDE) or not shutil.which("g++"):
         pytest.skip("needs the reference's sources, the CUDA headers and g++")
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    body = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
+    src = os.path.join(ROOT, "tests", "integration_stub.cpp")
+    body = open(src).read()
     assert "blamm_scan(" in body and "getNextOverlappingBlock" in body
     # the reference's build generates config.h (F77 name mangling); any definition will do here
     (tmp_path / "config.h").write_text("#define F77_FUNC(name,NAME) name ## _\n")
-    src = tmp_path / "stub.cpp"
-    src.write_text('#include "pwmscan.h"\n#include "blamm_gpu.h"\nusing namespace std;\n\n'
-                   "void PWMScan::scanThreadCUBLAS(int devID, size_t speciesID, ProgressIndicator& progInd,\n"
-                   "                               FastaBatch& seqBatch)\n{\n" + body + "}\n")
     cmd = ["g++", "-std=c++11", "-fsyntax-only", "-Wall", "-DHAVE_CONFIG_H", "-DHAVE_CUDA",
-           f"-I{tmp_path}", f"-I{REFERENCE_SRC}", f"-I{os.path.join(ROOT, 'include')}", f"-I{CUDA_INCLUDE}"]
+           f"-I{tmp_path}", f"-I{ref_src}", f"-I{os.path.join(ROOT, 'include')}", f"-I{CUDA_INCLUDE}"]
     # the reference's headers use these without including them under gcc 13
     for h in ("array", "mutex", "cassert", "limits", "stdexcept", "map", "future"):
         cmd += ["-include", h]
-    r = subprocess.run(cmd + [str(src)], capture_output=True, text=True)
+    r = subprocess.run(cmd + [src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
 
 

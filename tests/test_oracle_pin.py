@@ -26,7 +26,9 @@ def test_oracle_cli_matches_reference_fixtures(tmp_path, case):
     gc.compare(d, case, spec, what=("dict", "hist", "thresholds", "occ"))
 
 
-EXAMPLE = "/root/reference/example"
+import oracle_build  # oracle/oracle_build.py
+
+EXAMPLE = os.path.join(oracle_build.reference_dir(), "example")
 
 
 @pytest.mark.skipif(not (os.path.isdir(EXAMPLE) and os.path.exists(oracle.REF_CLI_PATH)),

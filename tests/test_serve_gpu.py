@@ -76,3 +76,43 @@ def test_admission_by_memory_budget_serialises_large_requests():
         want["col"] = sub[want["col"]]
         ok, msg = same_hits(g, want)
         assert ok, msg
+
+
+def test_admission_counts_the_buffers_slots_keep():
+    """Slots keep the device buffers of earlier requests; admission counts them, and when the
+    queue's head does not fit with nothing in flight the slots release theirs.  A budget a little
+    above one request's estimate keeps the committed bytes (requests in flight + kept buffers)
+    within it at every admission and completion, and every request still gets its hits."""
+    from blamm_gb300 import GpuScanner
+    P, lens, thr = make_bank(75, 40, 5, 20, rel=0.85)
+    reqs = _requests(np.random.default_rng(76), len(lens), 10)
+    sc = GpuScanner(0, "auto")  # how many bytes one slot keeps after a request
+    try:
+        sc.set_motifs(P, lens, thr)
+        b, r, _, _ = max(reqs, key=lambda q: len(q[0]))
+        sc.scan(b, r)
+        kept = sc.call_bytes()
+        assert kept > 0
+        sc.release_buffers()
+        assert sc.call_bytes() == 0
+        ok, msg = same_hits(sc.scan(b, r), oracle.scan(b, r, P, lens, thr))  # usable after the release
+        assert ok, msg
+    finally:
+        sc.close()
+    budget = 2 * kept + (24 << 20)
+    srv = Server(P, lens, thr[None, :], slots=4, hbm_budget=budget)
+    try:
+        ids = [srv.submit(b, r, c, 0) for b, r, c, _ in reqs]
+        got = [srv.take(i) for i in ids]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["peak_committed"] <= st["budget"]
+    assert st["bytes_held"] > 0
+    for (bases, runs, cols, _), g in zip(reqs, got):
+        sub = np.arange(len(lens)) if cols is None else cols
+        want = oracle.scan(bases, runs, P[sub], lens[sub], thr[sub])
+        want["col"] = sub[want["col"]]
+        ok, msg = same_hits(g, want)
+        assert ok, msg
