@@ -384,6 +384,44 @@ def emitted_score_error(hits, ref, npos: int) -> dict:
             "note": "the reference's own FP32 sum; error = FP32 rounding of the sequential sum"}
 
 
+def precision_other_configs(seed: int, npos: int = 2048) -> dict:
+    """Score error against FP64 on the other cases' shapes, each on a sample generated like the
+    case itself: the raw tensor-core sums (one and two BF16 terms) and the emitted scores."""
+    from blamm_gb300 import GpuScanner, workloads
+    from blamm_gb300._native import MotifBank
+    rng = np.random.default_rng([seed, 9])
+    cases = {}
+    w1 = workloads.two_sequences_1mbp(seed, seq_len=npos + 512)
+    cases["two_sequences_1mbp (32 motifs, L 6-20, iid A=T=0.3)"] = (w1.motifs, w1.sequences[0][1], 1e-4)
+    m3 = workloads.random_pfms(rng, 2000, 5, 30)
+    s3 = workloads.insert_n_runs(rng, workloads.markov2_bases(rng, 200_000, 0.41), 0.01)
+    b3, r3, _, _ = workloads.filtered_stream([("s", s3)])
+    cases["genome_1gbp (2000 motifs, L 5-30, 2nd-order Markov GC 0.41, N runs), p=1e-5"] = (m3, b3, 1e-5)
+    m4 = workloads.random_pfms(rng, 800, 6, 25)
+    cases["promoters_10k (800 motifs, L 6-25, GC 0.5)"] = (m4, workloads.iid_bases(rng, npos + 512, [0.25] * 4), 1e-4)
+    out = {}
+    for name, (motifs, bases, pv) in cases.items():
+        bases = np.ascontiguousarray(bases[:npos + 512])
+        counts = np.array([max(1, np.count_nonzero((bases | 0x20) == ord(c))) for c in "acgt"], dtype=np.uint64)
+        bank = MotifBank.from_pfms([p for _, p in motifs], revcompl=True)
+        bank.generate(counts, 0.25)
+        P, lens, _ = bank.matrix()
+        bgp = ((counts.astype(np.float32) + np.float32(0.25)) /
+               (np.float32(counts.sum()) + np.float32(1.0))).astype(np.float32)
+        thr = bank.pvalue_thresholds(bgp, pv)
+        ref = fp64_window_scores(bases, P, lens, npos)
+        res = {}
+        for mode in ("bf16x2", "bf16"):
+            sc = GpuScanner(0, mode)
+            sc.set_motifs(P, lens, thr)
+            res["mma_" + mode] = mma_score_error(sc, bases, P, lens, ref, npos)
+            if mode == "bf16x2":
+                res["emitted"] = emitted_score_error(sc.scan(bases, np.zeros(1, dtype=np.int64)), ref, npos)
+            sc.close()
+        out[name] = res
+    return out
+
+
 # ------------------------------------------------------------------ serving
 def run_serve(a) -> dict:
     """Serving through the scan service (include/blamm_serve.h): a resident bank of
@@ -776,6 +814,7 @@ def run_ours(a, rank, world, local):
             precision["mma_" + mode] = mma_score_error(sc, bases, P, lens, ref, npos)
         sc.set_mode(a.mode)
         precision["emitted"] = emitted_score_error(hits_on_device(nh), ref, npos)
+        precision["other_cases"] = precision_other_configs(a.seed)
 
     # ---- roofline of the dominant kernel (tcgen05 scan)
     peak, peak_src = peaks()

@@ -48,7 +48,8 @@ struct Request {
 struct Slot {
     blamm_ctx *ctx = nullptr;
     int set = -1;
-    int64_t held = 0;  // device bytes the context keeps between requests
+    int64_t held = 0;  // device bytes the context keeps between requests (measured)
+    int64_t need = 0;  // estimate of the request in flight on the slot (0: idle)
     std::thread th;
 };
 
@@ -88,6 +89,17 @@ int fail(blamm_server *s, int code, const char *fmt, ...)
         s->err = buf;
     }
     return code;
+}
+
+// Device bytes committed by the slots other than `except` (-1: all): a slot in flight holds
+// the larger of its kept buffers and its request's estimate (the request reuses them), an idle
+// slot its kept buffers.  The caller holds the server's lock.
+int64_t committed(const blamm_server *s, int except)
+{
+    int64_t c = 0;
+    for (size_t k = 0; k < s->slots.size(); ++k)
+        if ((int)k != except) c += std::max(s->slots[k].held, s->slots[k].need);
+    return c;
 }
 
 // Device bytes a request holds while it runs: raw and packed stream, the one-hot entries
@@ -149,19 +161,19 @@ void slot_loop(blamm_server *s, int k)
                 if (s->stop) return true;
                 if (s->release && slot.held > 0) return true;  // give the kept buffers back
                 if (s->queue.empty()) return false;
-                // first in, first out: the head is admitted when it fits beside the requests in
-                // flight and the buffers the other slots keep (this slot's are reused by it)
+                // first in, first out: the head is admitted when it fits beside what the other
+                // slots commit (this slot's kept buffers are reused by it)
                 const int64_t need = s->queue.front()->need;
-                if (s->in_flight_bytes + s->held_bytes - slot.held + need <= s->budget) return true;
+                if (committed(s, k) + std::max(slot.held, need) <= s->budget) return true;
                 if (s->in_flight_bytes == 0 && !s->release) {
                     s->release = true;  // nothing runs: the slots release what they keep
                     s->cv_work.notify_all();
                 }
-                return s->in_flight_bytes == 0 && s->held_bytes == slot.held;  // every other slot released
+                return s->in_flight_bytes == 0 && committed(s, k) == 0;  // every other slot released
             });
             if (s->stop) return;
-            if (s->release && slot.held > 0 && s->in_flight_bytes + s->held_bytes - slot.held +
-                                                       (s->queue.empty() ? 0 : s->queue.front()->need) > s->budget) {
+            if (s->release && slot.held > 0 &&
+                (s->queue.empty() || committed(s, k) + std::max(slot.held, s->queue.front()->need) > s->budget)) {
                 const int64_t had = slot.held;
                 lk.unlock();
                 blamm_release_buffers(slot.ctx);
@@ -179,15 +191,28 @@ void slot_loop(blamm_server *s, int k)
             r = s->queue.front();
             s->queue.pop_front();
             s->in_flight_bytes += r->need;
-            // committed: the requests in flight plus the other slots' kept buffers
-            s->st.peak_committed =
-                std::max(s->st.peak_committed, s->in_flight_bytes + s->held_bytes - slot.held);
+            slot.need = r->need;
+            s->st.peak_committed = std::max(s->st.peak_committed, committed(s, -1));
             r->t_admit = Clock::now();
         }
         s->cv_work.notify_all();  // the next request may fit too
         run_request(s, slot, *r);
         int64_t kept = 0;
         blamm_ctx_call_bytes(slot.ctx, &kept);
+        bool over = false;
+        {
+            // the slot now holds what its context keeps, which may exceed the request's estimate:
+            // if the slots' commitments no longer fit, this (now idle) slot gives its buffers back
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->held_bytes += kept - slot.held;
+            slot.held = kept;
+            slot.need = 0;
+            over = committed(s, -1) > s->budget;
+        }
+        if (over) {
+            blamm_release_buffers(slot.ctx);
+            blamm_ctx_call_bytes(slot.ctx, &kept);
+        }
         {
             std::lock_guard<std::mutex> lk(s->mu);
             r->t_done = Clock::now();
@@ -195,7 +220,6 @@ void slot_loop(blamm_server *s, int k)
             s->in_flight_bytes -= r->need;
             s->held_bytes += kept - slot.held;
             slot.held = kept;
-            s->st.peak_committed = std::max(s->st.peak_committed, s->in_flight_bytes + s->held_bytes);
             if (r->status == BLAMM_OK) {
                 s->st.completed += 1;
                 s->st.bases += (int64_t)r->bases.size();

@@ -19,10 +19,11 @@
  *     slots keep leave of the budget.  Admission is first in, first out.  A
  *     slot's context keeps the device buffers of the largest request it has run
  *     (they are reused: the slot's own kept bytes count toward its next request);
- *     their size is measured after every request.  When the queue's head does
- *     not fit and nothing is in flight, every slot releases its kept buffers
- *     (blamm_release_buffers), so a request that fits the budget alone always
- *     runs;
+ *     their size is measured after every request, and a slot whose kept
+ *     buffers no longer fit beside the others' commitments releases them
+ *     (blamm_release_buffers).  When the queue's head does not fit and nothing
+ *     is in flight, every slot releases its kept buffers, so a request that fits
+ *     the budget alone always runs;
  *   - results: the hits of a request are the same alone and in any mix (each
  *     request has its own context; scores are exact FP32, see blamm_gpu.h).
  *
@@ -55,7 +56,8 @@ typedef struct {
     double bp_columns;        /* sum over completed requests of positions x columns */
     int64_t bytes_in_flight;  /* admitted estimate */
     int64_t bytes_held;       /* device bytes the slots' contexts keep between requests */
-    int64_t peak_committed;   /* largest in-flight estimate + kept bytes seen at admission or completion */
+    int64_t peak_committed;   /* largest commitment at an admission: per slot the larger of its kept
+                                 bytes and its request's estimate */
     int64_t budget;
 } blamm_server_stats;
 

@@ -108,8 +108,8 @@ def test_admission_counts_the_buffers_slots_keep():
     finally:
         srv.close()
     assert st["completed"] == len(reqs) and st["failed"] == 0
-    assert st["peak_committed"] <= st["budget"]
-    assert st["bytes_held"] > 0
+    assert 0 < st["peak_committed"] <= st["budget"]
+    assert st["bytes_held"] <= st["budget"]
     for (bases, runs, cols, _), g in zip(reqs, got):
         sub = np.arange(len(lens)) if cols is None else cols
         want = oracle.scan(bases, runs, P[sub], lens[sub], thr[sub])
