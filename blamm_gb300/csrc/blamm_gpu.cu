@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <mutex>
@@ -40,6 +41,9 @@ using namespace blamm;
 
 static_assert(sizeof(blamm_hit) == sizeof(HitRec), "hit record layout");
 
+// Default scan window (positions): see launch_tc_windows.
+constexpr int64_t kEWindowDefault = int64_t(16) << 20;
+
 struct blamm_ctx {
     int device = 0;
     int sm_count = 0;
@@ -53,6 +57,7 @@ struct blamm_ctx {
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
     int debug_stall = 0;                  // test hook: make the scan kernel's first wait run out
+    int64_t ewindow = 0;                  // positions per tensor-core scan window (one-hot entry array)
 
     // motif bank (host copy); `active` lists the columns scanned (all when empty)
     int ncols = 0, p_rows = 0, lmax = 0;
@@ -427,6 +432,10 @@ int blamm_ctx_create(int device, blamm_ctx **out)
             return fail(ctx, BLAMM_ERR_UNSUPPORTED, "compute capability %d.%d is not sm_100-class",
                         prop.major, prop.minor);
         ctx->sm_count = prop.multiProcessorCount;
+        // scan window (positions, a multiple of 128): BLAMM_SCAN_WINDOW overrides the default
+        ctx->ewindow = kEWindowDefault;
+        if (const char *w = std::getenv("BLAMM_SCAN_WINDOW"))
+            ctx->ewindow = std::max<int64_t>(kBM, std::atoll(w) / kBM * kBM);
         ctx->max_smem = (int)prop.sharedMemPerBlockOptin;
         cudaFuncAttributes fa;
         // fails if no sm_103a image fits
@@ -653,8 +662,7 @@ static int ensure_plan(blamm_ctx *ctx)
 // array holds one window (64 MB) whatever the stream length.  A window's scan reads up to
 // entry (its positions) + 127 + 4 * 64 + 2, and e16_kernel reads base i + 1 of the padded
 // stream: entries = positions + kStreamPad - 64 stay inside both.
-constexpr int64_t kEWindow = int64_t(4) << 20;
-static int64_t e16_entries(int64_t n) { return std::min(n, kEWindow) + kStreamPad - 64; }
+static int64_t e16_entries(const blamm_ctx *ctx, int64_t n) { return std::min(n, ctx->ewindow) + kStreamPad - 64; }
 
 static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
 {
@@ -669,7 +677,7 @@ static int launch_pack(blamm_ctx *ctx, const char *d_bases, int64_t n)
                                                                nwords32, ctx->lower_scores);
     CK(cudaGetLastError());
     if (ctx->mode != BLAMM_MODE_FP32) {
-        rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(n));
+        rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(ctx, n));
         if (rc) return rc;
     }
     return BLAMM_OK;
@@ -769,7 +777,7 @@ static void launch_tc(const TcParams &p, bool dump, int grid, uint32_t smem, cud
 static int launch_tc_windows(blamm_ctx *ctx, TcParams p, const uint32_t *seq2, const uint32_t *zmask, uint4 *e16,
                              int64_t n, bool dump, uint32_t smem, int *launches, int *grid_out)
 {
-    const int64_t n_mtiles = (n + kBM - 1) / kBM, wt = kEWindow / kBM;
+    const int64_t n_mtiles = (n + kBM - 1) / kBM, wt = std::max<int64_t>(1, ctx->ewindow / kBM);
     int gmax = 0;
     for (int64_t m0 = 0; m0 < n_mtiles; m0 += wt) {
         const int64_t mt = std::min(wt, n_mtiles - m0), base = m0 * kBM;
@@ -1154,7 +1162,7 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
     if ((rc = ensure(ctx, &ctx->d_zmask, &ctx->cap_zmask, (size_t)nwords32))) return rc;
     if (tc) {
         if ((rc = ensure_plan(ctx))) return rc;
-        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(span)))) return rc;
+        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(ctx, span)))) return rc;
         // candidates: four times the usual first guess for a chunk (a chunk that still
         // overflows sends the whole call to the synchronous path)
         const double want = (double)record_slots_guess(ctx, span, 250.0);
@@ -1261,7 +1269,7 @@ static int scan_host_async_steps(blamm_ctx *ctx, const char *bases, int64_t n, c
     total.launches = 0;
     for (int64_t k = 0; k < nchunks; ++k) {  // packing + scan (+ rescoring and a one-hot build per window)
         const int64_t len = std::min(n, (k + 1) * kPipeChunk + ov) - k * kPipeChunk;
-        total.launches += (int32_t)(tc ? 2 + 2 * ((len + kEWindow - 1) / kEWindow) : 2);
+        total.launches += (int32_t)(tc ? 2 + 2 * ((len + ctx->ewindow - 1) / ctx->ewindow) : 2);
     }
     int status = 0;
     for (int64_t k = 0; k < nchunks; ++k) {
@@ -1744,7 +1752,7 @@ int blamm_reserve(blamm_ctx *ctx, int64_t max_positions, int64_t max_candidates)
     if (rc) return rc;
     if (ctx->mode != BLAMM_MODE_FP32) {
         if ((rc = ensure_plan(ctx))) return rc;
-        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(max_positions)))) return rc;
+        if ((rc = ensure(ctx, &ctx->d_e16, &ctx->cap_e16, (size_t)e16_entries(ctx, max_positions)))) return rc;
         // record slots: at most one record per candidate, plus the blocks the warps reserve
         const int64_t slots = std::min(max_candidates + record_slots_reserved(ctx->sm_count), kMaxRecordSlots);
         if (slots > ctx->cand_cap) {
@@ -1771,7 +1779,7 @@ int blamm_scan_enqueue(blamm_ctx *ctx, const char *d_bases, int64_t n, const int
     const bool tc = ctx->mode != BLAMM_MODE_FP32;
     const int terms = mode_terms(ctx);
     if (tc && (!(ctx->plan_valid && ctx->plan_terms == terms) || ctx->cand_cap <= 0 ||
-               (size_t)e16_entries(n) > ctx->cap_e16))
+               (size_t)e16_entries(ctx, n) > ctx->cap_e16))
         return fail(ctx, BLAMM_ERR_STATE, "blamm_scan_enqueue: call blamm_reserve after changing the bank, "
                                           "columns, thresholds or mode");
     if (n > 0 && (!d_bases || !d_run_start || nruns <= 0 || (hit_cap > 0 && !d_hits)))
