@@ -47,6 +47,7 @@ def args_parse():
     ap.add_argument("--cpu-sample", type=int, default=8_000_000, help="bases in a CPU-baseline sample")
     ap.add_argument("--no-modes", action="store_true", help="skip the bf16 / fp32 comparison runs")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-cli", action="store_true", help="skip the end-to-end command-line measurement")
     ap.add_argument("--mode", default="auto", choices=["auto", "bf16", "bf16x2"],
                     help="headline arithmetic: auto (the library default, autotuned on a sample) or a fixed "
                          "term count with the default tile plan (no autotuner launches, for profiling)")
@@ -177,15 +178,15 @@ def peaks():
 
 
 def profile_traffic(positions: int, terms: int):
-    """DRAM bytes of one scan-kernel launch (the instance for `terms` BF16 terms), scaled by
-    positions from the committed ncu summary."""
+    """DRAM bytes of one scan-kernel launch (the instance for `terms` BF16 terms) over
+    `positions` positions, scaled by positions from the committed ncu capture."""
     path = os.path.join(ROOT, "profiles", "scan_tc_traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    b = d["dram_bytes_by_terms"].get(str(terms))
-    return None if b is None else int(b * positions / d["positions"])
+    c = d["by_terms"].get(str(terms))
+    return None if c is None else int(c["dram_bytes"] * positions / c["positions"])
 
 
 def hit_digest(h: np.ndarray) -> tuple[int, int]:
@@ -285,6 +286,59 @@ def cli_e2e(wl, bases, sample: int) -> dict:
                 "occurrence_lines": lines,
                 "sample": f"first {sample} bp (FASTA, {len(seqs)} sequences) x {2 * len(wl.motifs)} columns: "
                           "read, scan, write the occurrence file"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def cli_ours(wl, pvalue: float) -> dict:
+    """The drop-in command line on the whole workload, end to end: the FASTA files of the
+    genome, `blamm dict` (timed), `blamm hist` (untimed, run once as the workflow does) and
+    `blamm scan -rc -pt <p>` (timed) writing the occurrence file; the scan's phase split
+    (BLAMM_TIMING) with the default GPU FASTA reader, and the scan's time with the host
+    reader beside it."""
+    import re
+    import shutil
+    import subprocess
+    import tempfile
+    from blamm_gb300 import workloads
+    from blamm_gb300._native import CLI_PATH
+    d = tempfile.mkdtemp(prefix="blamm_cli_ours_")
+    try:
+        workloads.write_case(d, {"genome": [("genome.fa", wl.sequences)]}, wl.motifs)
+        workloads.write_settings(os.path.join(d, "settings.cnf"))
+        out = {}
+
+        def run(args, env=None):
+            t0 = time.perf_counter()
+            r = subprocess.run([CLI_PATH] + args, cwd=d, capture_output=True, text=True,
+                               env=dict(os.environ, **(env or {})))
+            dt = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise RuntimeError(f"blamm {args[0]} failed: {r.stderr[-500:]}")
+            return dt, r.stderr
+
+        out["dict_seconds"], _ = run(["dict", "sequences.mf"])
+        out["dict_seconds_host_reader"], _ = run(["dict", "sequences.mf"], {"BLAMM_FASTA_READER": "host"})
+        run(["hist", "motifs.jaspar", "sequences.mf"])
+        scan = ["scan", "-rc", "-pt", str(pvalue), "motifs.jaspar", "sequences.mf"]
+        run(scan)  # warm: page cache, GPU context
+        out["scan_seconds"], err = run(scan, {"BLAMM_TIMING": "1"})
+        m = re.search(r"timing: (.*)", err)
+        out["scan_phases"] = m.group(1).strip() if m else None
+        with open(os.path.join(d, "occurrences.txt"), "rb") as f:
+            out["occurrence_lines"] = sum(1 for _ in f)
+        out["occurrence_bytes"] = os.path.getsize(os.path.join(d, "occurrences.txt"))
+        out["scan_seconds_host_reader"], err = run(scan, {"BLAMM_FASTA_READER": "host", "BLAMM_TIMING": "1"})
+        m = re.search(r"timing: (.*)", err)
+        out["scan_phases_host_reader"] = m.group(1).strip() if m else None
+        bp = sum(len(s) for _, s in wl.sequences)
+        out["value"] = bp * 2 * len(wl.motifs) / out["scan_seconds"]
+        out["unit"] = UNIT
+        out["workload"] = (f"{bp} bp FASTA ({len(wl.sequences)} sequences, 60-base lines) x "
+                           f"{2 * len(wl.motifs)} columns -> occurrence file")
+        return out
+    except Exception as e:  # reported, not fatal to the bench line
+        return {"unavailable": str(e)[:300]}
     finally:
         shutil.rmtree(d, ignore_errors=True)
 
@@ -820,7 +874,9 @@ def run_ours(a, rank, world, local):
     peak, peak_src = peaks()
     kern_ms = float(np.mean(scan_ms))
     achieved = n * flops_per_bp / (kern_ms / 1e3) / 1e12
-    traffic = profile_traffic(n, terms)
+    # a step = packing + (one-hot entries + scan) per scan window + rescoring
+    scan_launches = max(1, (launches // a.steps - 2) // 2)
+    traffic = profile_traffic(int(round(n / scan_launches)), terms)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -850,9 +906,12 @@ def run_ours(a, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "note": f"algorithmic flops = 8 * sum(L) = {flops_per_bp:.0f} per bp per launch over "
-                             f"{n} bp; {terms} BF16 term(s) issue {terms} MMA(s) per flop (ceiling "
-                             f"{1 / terms:g} before padding and the bias MMA); peak {peak_src}"},
+                     "scan_launches_per_step": scan_launches,
+                     "note": f"algorithmic flops = 8 * sum(L) = {flops_per_bp:.0f} per bp over {n} bp in "
+                             f"{scan_launches} window launch(es) per step, divided by their summed time; "
+                             f"traffic per launch ({n / scan_launches:.0f} positions); {terms} BF16 term(s) "
+                             f"issue {terms} MMA(s) per flop (ceiling {1 / terms:g} before padding and the "
+                             f"bias MMA); peak {peak_src}"},
         "modes": modes,
         "score_error_vs_fp64": precision,
         "clocks": clk,
@@ -863,6 +922,8 @@ def run_ours(a, rank, world, local):
         if line["serve"]["open_loop"]:
             line["serve_p50_ms"] = line["serve"]["open_loop"][-1]["p50_ms"]
             line["serve_p99_ms"] = line["serve"]["open_loop"][-1]["p99_ms"]
+    if rank == 0 and world == 1 and not a.no_cli and a.workload == "genome_100mbp":
+        line["cli"] = cli_ours(wl, wl.pvalue)
     if rank == 0 and world == 1:
         v, cores, dt, ohits = cpu_sample_scan(bases, runs, P, lens, thr, min(a.cpu_sample, n))
         # parity on the headline workload: the GPU headline hits of every window inside the sample

@@ -96,6 +96,9 @@ def gpu_lib() -> C.CDLL:
     lib.blamm_get_terms.argtypes = [vp]
     lib.blamm_ctx_call_bytes.argtypes = [vp, C.POINTER(i64)]
     lib.blamm_release_buffers.argtypes = [vp]
+    lib.blamm_stream_load_fasta.argtypes = [vp, vp, i64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), vp]
+    lib.blamm_stream_tables.argtypes = [vp, vp, vp, vp, vp]
+    lib.blamm_scan_stream.argtypes = [vp, i64, i64, vp, i64, vp, i64, C.POINTER(i64)]
     for name in ("blamm_ctx_create", "blamm_set_mode", "blamm_set_motifs", "blamm_set_thresholds",
                  "blamm_scan", "blamm_scan_device", "blamm_filter_score", "blamm_last_stats",
                  "blamm_debug_scores", "blamm_guard_band", "blamm_ctx_stream", "blamm_device_count",
@@ -104,7 +107,8 @@ def gpu_lib() -> C.CDLL:
                  "blamm_reserve", "blamm_scan_enqueue", "blamm_scan_graph_create", "blamm_scan_graph_launch",
                  "blamm_autotune", "blamm_theoretical_hist", "blamm_device_memory", "blamm_set_plan_options",
                  "blamm_get_plan_options", "blamm_fasta_parse_device", "blamm_debug_stall", "blamm_get_terms",
-                 "blamm_ctx_call_bytes", "blamm_release_buffers"):
+                 "blamm_ctx_call_bytes", "blamm_release_buffers", "blamm_stream_load_fasta",
+                 "blamm_stream_tables", "blamm_scan_stream"):
         getattr(lib, name).restype = C.c_int
     _ = i32
     _gpu = lib
@@ -126,6 +130,7 @@ class GpuScanner:
             raise BlammError(rc, f"cannot create a context on device {device}")
         self.h = h
         self.ncols = 0
+        self._stream = (0, 0, 0)
         self.set_mode(mode)
 
     def close(self) -> None:
@@ -263,6 +268,39 @@ class GpuScanner:
             _ptr(nucl) if nucl is not None else None))
         return nb.value, nr.value, ns.value
 
+    def stream_load_fasta(self, raw: bytes) -> tuple[int, int, int, np.ndarray]:
+        """FASTA text (host bytes) parsed on the device into the resident stream:
+        (bases, runs, sequences, A/C/G/T counts)."""
+        buf = np.frombuffer(raw, dtype=np.uint8) if len(raw) else np.zeros(1, dtype=np.uint8)
+        nb, nr, ns = C.c_int64(), C.c_int64(), C.c_int64()
+        nucl = np.zeros(4, dtype=np.uint64)
+        self._check(self.lib.blamm_stream_load_fasta(self.h, _ptr(buf), len(raw), C.byref(nb), C.byref(nr),
+                                                     C.byref(ns), _ptr(nucl)))
+        self._stream = (nb.value, nr.value, ns.value)
+        return nb.value, nr.value, ns.value, nucl
+
+    def stream_tables(self) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+        """The resident stream's run table (start, sequence, position in it) and header offsets."""
+        _, nr, ns = self._stream
+        rs, rq, rp = (np.zeros(max(nr, 1), dtype=np.int64) for _ in range(3))
+        hp = np.zeros(max(ns, 1), dtype=np.int64)
+        self._check(self.lib.blamm_stream_tables(self.h, _ptr(rs), _ptr(rq), _ptr(rp), _ptr(hp)))
+        return rs[:nr], rq[:nr], rp[:nr], hp[:ns]
+
+    def scan_stream(self, begin: int, n: int, run_start: np.ndarray, hit_cap: int | None = None) -> np.ndarray:
+        """Scan positions [begin, begin + n) of the resident stream (runs relative to begin)."""
+        runs = np.ascontiguousarray(run_start, dtype=np.int64)
+        cap = hit_cap if hit_cap is not None else max(1 << 16, n * max(self.ncols, 1) // 2000)
+        while True:
+            out = np.empty(max(cap, 1), dtype=HIT_DTYPE)
+            nh = C.c_int64(0)
+            rc = self.lib.blamm_scan_stream(self.h, begin, n, _ptr(runs), len(runs), _ptr(out), cap, C.byref(nh))
+            if rc == BLAMM_ERR_OVERFLOW and hit_cap is None:
+                cap = int(nh.value * 1.1) + 1024
+                continue
+            self._check(rc)
+            return out[:nh.value].copy()
+
     def debug_stall(self, enable: bool, wait_limit_cycles: int = 0) -> None:
         """Failure-path test hook (see blamm_debug_stall)."""
         self._check(self.lib.blamm_debug_stall(self.h, int(enable), wait_limit_cycles))
@@ -283,6 +321,7 @@ class GpuScanner:
 
     def release_buffers(self) -> None:
         self._check(self.lib.blamm_release_buffers(self.h))
+        self._stream = (0, 0, 0)
 
     def terms(self) -> int:
         """BF16 terms of the tensor-core scan in the current mode (0 in FP32 mode)."""

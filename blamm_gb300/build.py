@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
             "-Wno-unused-parameter"]
 HOST_SRCS = ["motif.cpp", "sequence.cpp", "species.cpp", "histogram.cpp",
-             "scan.cpp", "host_capi.cpp", "serve.cpp", "format.cpp"]
+             "scan.cpp", "host_capi.cpp", "serve.cpp", "format.cpp", "ingest.cpp"]
 
 
 def _nvcc() -> str:

@@ -126,6 +126,13 @@ struct blamm_ctx {
     cudaEvent_t done_ev[2] = {nullptr, nullptr};  // per input buffer: its chunk's kernels are done
     unsigned long long *h_chunk_counts = nullptr;  // pinned, 4 per chunk: candidates, hits, status
     size_t cap_h_chunk_counts = 0;
+    // resident stream (blamm_stream_load_fasta): FASTA text, filtered bases, run table
+    // (stream position, sequence index, position in the sequence), header offsets
+    char *d_raw = nullptr, *d_stream = nullptr;
+    size_t cap_raw = 0, cap_stream = 0;
+    int64_t *d_srun[3] = {nullptr, nullptr, nullptr}, *d_shdr = nullptr;
+    size_t cap_srun[3] = {0, 0, 0}, cap_shdr = 0;
+    int64_t stream_n = 0, stream_nruns = 0, stream_nseqs = 0;
     bool prof_on = false;
     long long *d_prof = nullptr;
     std::vector<long long> prof;  // last scan's role timing, 32 counters per CTA
@@ -210,6 +217,10 @@ inline uint16_t bf16_bits_exact(double v)
     return (uint16_t)(u >> 16);  // exact: v has <= 8 significant bits
 }
 
+// A tile whose longest motif has length L = 4g-3 or 4g-2 leaves motif positions 4g-2 and
+// 4g-1 (the second K core of its last k-step) unused: the bias rides there.
+inline bool bias_folds(int L) { return L % 4 == 1 || L % 4 == 2; }
+
 }  // namespace
 
 static int build_plan(blamm_ctx *ctx, int terms)
@@ -247,8 +258,9 @@ static int build_plan(blamm_ctx *ctx, int terms)
         return fail(ctx, BLAMM_ERR_UNSUPPORTED, "motif bank does not fit shared memory");
 
     // DP over sorted columns: tile = contiguous run of sorted columns.
-    // Per-job cycle model: MMA = (terms*g + 1)*N/2 (bias step included), epilogue ~ N,
-    // plus a fixed cost per job (E build, hand-offs).
+    // Per-job cycle model: MMA = (terms*g + bias)*N/2, epilogue ~ N, plus a fixed cost per
+    // job (hand-offs); the bias MMA is folded into the last k-step when the tile's longest
+    // motif leaves that k-step's second K core unused.
     const double kInf = 1e300;
     std::vector<double> f(nsel + 1, kInf);
     std::vector<int> from(nsel + 1, -1);
@@ -259,10 +271,11 @@ static int build_plan(blamm_ctx *ctx, int terms)
     for (int j = 1; j <= nsel; ++j) {
         const int L = ctx->len[order[j - 1]];
         const int g = std::max(1, (L + 3) / 4);
+        const int bias = bias_folds(L) ? 0 : 1;
         for (int N = 32; N <= 256; N += 32) {
             if (N > nmax_for(g)) break;
             const int i = std::max(0, j - N);
-            const double mma = (terms * g + 1) * N / 2.0, epi = 1.0 * N;
+            const double mma = (terms * g + bias) * N / 2.0, epi = 1.0 * N;
             const double cost = std::max(std::max(mma, epi), 300.0) + ctx->plan_job_cost;
             if (f[i] + cost < f[j]) {
                 f[j] = f[i] + cost;
@@ -323,9 +336,10 @@ static int build_plan(blamm_ctx *ctx, int terms)
 
     // tiles, slots, B buffer.  B term layout (canonical no-swizzle K-major):
     // element (column i, K index kk) of a tile with g motif k-steps sits at
-    // ((i/8 * 2(g+1) + kk/8) * 8 + i%8) * 8 + kk%8; k-step g (K indices
-    // 16g..16g+15) holds, in the hi term, the bias: -T split into three
-    // BF16-exact pieces on the column's grid.
+    // ((i/8 * 2(g+1) + kk/8) * 8 + i%8) * 8 + kk%8.  The hi term holds the bias,
+    // -T split into three BF16-exact pieces on the column's grid, in K indices
+    // 16g..16g+2 (the bias MMA's k-step) or, in a folded tile, 16g-8..16g-6 (the
+    // second K core of k-step g-1, which no motif of the tile reaches).
     std::vector<TileDesc> tiles;
     std::vector<int32_t> slot_col;
     std::vector<uint8_t> bbuf;
@@ -343,6 +357,8 @@ static int build_plan(blamm_ctx *ctx, int terms)
         td.n = N;
         td.g = g;
         td.b_bytes = N * 16 * (g + 1) * 2;
+        td.fold = bias_folds(L) ? 1 : 0;
+        const int kb = td.fold ? 16 * g - 8 : 16 * g;  // K index of the first bias piece
         size_t off = (bbuf.size() + 1023) / 1024 * 1024;
         td.b_off = (int64_t)off;
         bbuf.resize(off + (size_t)td.b_bytes * terms, 0);
@@ -371,7 +387,7 @@ static int build_plan(blamm_ctx *ctx, int terms)
             const int64_t pc = rem - pb * 256;
             const int64_t pieces[3] = {pa * 65536, pb * 256, pc};
             for (int s = 0; s < 3; ++s)
-                if (pieces[s] != 0) b_hi[elem(i, 16 * g + s)] = bf16_bits_exact(-std::ldexp((double)pieces[s], -(k + 8)));
+                if (pieces[s] != 0) b_hi[elem(i, kb + s)] = bf16_bits_exact(-std::ldexp((double)pieces[s], -(k + 8)));
             if (c < 0) continue;
             const uint32_t o = ctx->colq_off[c], nk = ctx->colq_off[c + 1] - o;
             for (uint32_t kk = 0; kk < nk; ++kk) {
@@ -479,7 +495,8 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
                     ctx->d_slot_col, ctx->d_prof, ctx->d_bases, ctx->d_seq2, ctx->d_zmask, ctx->d_e16,
                     ctx->d_runs,   ctx->d_cand,  ctx->d_hits,     ctx->d_counters, ctx->d_status,
                     ctx->d_active, ctx->d_chunk_bases[0], ctx->d_chunk_bases[1], ctx->d_chunk_runs[0],
-                    ctx->d_chunk_runs[1]};
+                    ctx->d_chunk_runs[1], ctx->d_raw, ctx->d_stream, ctx->d_srun[0], ctx->d_srun[1],
+                    ctx->d_srun[2], ctx->d_shdr};
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     for (void *b : bufs)
         if (b) cudaFree(b);
@@ -498,12 +515,14 @@ void blamm_ctx_destroy(blamm_ctx *ctx)
 }
 
 // Device bytes of the per-call buffers (stream, packed stream, one-hot window, run table,
-// candidate records, hits, pipeline chunks); the motif bank and its plan are not counted.
+// candidate records, hits, pipeline chunks, resident stream); the motif bank and its plan
+// are not counted.
 static int64_t call_buffer_bytes(const blamm_ctx *ctx)
 {
     return (int64_t)(ctx->cap_bases + 4 * ctx->cap_words32 + 4 * ctx->cap_zmask + 16 * ctx->cap_e16 +
                      8 * ctx->cap_runs + 8 * (ctx->cap_chunk_runs[0] + ctx->cap_chunk_runs[1]) +
-                     ctx->cap_chunk_bases[0] + ctx->cap_chunk_bases[1]) +
+                     ctx->cap_chunk_bases[0] + ctx->cap_chunk_bases[1] + ctx->cap_raw + ctx->cap_stream +
+                     8 * (ctx->cap_srun[0] + ctx->cap_srun[1] + ctx->cap_srun[2] + ctx->cap_shdr)) +
            16 * ctx->cand_cap + (int64_t)sizeof(blamm_hit) * ctx->hits_cap;
 }
 
@@ -534,6 +553,11 @@ int blamm_release_buffers(blamm_ctx *ctx)
         drop(&ctx->d_chunk_bases[b], &ctx->cap_chunk_bases[b]);
         drop(&ctx->d_chunk_runs[b], &ctx->cap_chunk_runs[b]);
     }
+    drop(&ctx->d_raw, &ctx->cap_raw);
+    drop(&ctx->d_stream, &ctx->cap_stream);
+    for (int k = 0; k < 3; ++k) drop(&ctx->d_srun[k], &ctx->cap_srun[k]);
+    drop(&ctx->d_shdr, &ctx->cap_shdr);
+    ctx->stream_n = ctx->stream_nruns = ctx->stream_nseqs = 0;
     if (ctx->d_cand) cudaFreeAsync(ctx->d_cand, ctx->stream);
     ctx->d_cand = nullptr;
     ctx->cand_cap = 0;
@@ -2060,21 +2084,13 @@ static cudaError_t device_scan(cudaStream_t st, int64_t *v, int64_t n, int64_t *
     return cudaGetLastError();
 }
 
-extern "C" {
-
-int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
-                             int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
-                             int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts)
+// FASTA text on the device -> filtered stream, run table and header offsets.  Outputs go
+// to the caller's buffers, or (resident: the caller's pointers are null) into the
+// context's resident-stream buffers, sized once the counts are known.
+static int fasta_parse(blamm_ctx *ctx, const char *d_raw, int64_t nraw, bool resident, char *d_bases,
+                       int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *d_header_pos,
+                       int64_t *n_bases, int64_t *nruns, int64_t *nseqs, uint64_t *nucl_counts)
 {
-    const NvtxRange nvtx_range("blamm_fasta_parse_device");
-    if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs) return BLAMM_ERR_ARG;
-    *n_bases = *nruns = *nseqs = 0;
-    if (nucl_counts)
-        for (int b = 0; b < 4; ++b) nucl_counts[b] = 0;
-    if (nraw == 0) return BLAMM_OK;
-    if (!d_raw || !d_bases || !d_run_start || !d_run_seq || !d_run_seqpos || !d_header_pos)
-        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
-    CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     const size_t n = (size_t)nraw, sw = scan_scratch_words(nraw);
     // four per-byte arrays (line starts, header count, sequence characters, stream bases),
@@ -2082,6 +2098,8 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     int64_t *A = nullptr, *B = nullptr, *Cc = nullptr, *D = nullptr, *sc0 = nullptr, *scr = nullptr;
     int *bad = nullptr;
     unsigned long long *nucl = nullptr;
+    int64_t *bseq = nullptr, *bpos = nullptr;
+    int rc = BLAMM_OK;
     cudaError_t e = cudaMallocAsync(&A, 8 * n, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&B, 8 * n, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&Cc, 8 * n, st);
@@ -2112,32 +2130,46 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     if (e == cudaSuccess) e = cudaMemcpyAsync(&badh, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     const int64_t ns = tot[0], nb = tot[1];
-    if (e == cudaSuccess && !badh) {
+    const bool go = e == cudaSuccess && !badh;
+    if (go && resident) {
+        rc = ensure(ctx, &ctx->d_shdr, &ctx->cap_shdr, (size_t)std::max<int64_t>(ns, 1));
+        if (!rc) rc = ensure(ctx, &ctx->d_stream, &ctx->cap_stream, (size_t)std::max<int64_t>(nb, 1));
+        d_header_pos = ctx->d_shdr;
+        d_bases = ctx->d_stream;
+    }
+    if (go && !rc) {
         ingest_headers_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, B, Cc, sc0, d_header_pos);
         e = cudaGetLastError();
     }
-    int64_t *bseq = nullptr, *bpos = nullptr;
-    if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bseq, 8 * (size_t)nb, st);
-    if (e == cudaSuccess && !badh && nb > 0) e = cudaMallocAsync(&bpos, 8 * (size_t)nb, st);
-    if (e == cudaSuccess && !badh && nb > 0) {
+    const bool have = go && !rc && nb > 0;
+    if (have && e == cudaSuccess) e = cudaMallocAsync(&bseq, 8 * (size_t)nb, st);
+    if (have && e == cudaSuccess) e = cudaMallocAsync(&bpos, 8 * (size_t)nb, st);
+    if (have && e == cudaSuccess) {
         ingest_bases_kernel<<<grid, 256, 0, st>>>(d_raw, nraw, A, B, Cc, D, sc0, d_bases, bseq, bpos, nucl);
         e = cudaGetLastError();
     }
     unsigned long long nh[4] = {0, 0, 0, 0};
-    if (e == cudaSuccess && !badh && nb > 0 && nucl_counts)
-        e = cudaMemcpyAsync(nh, nucl, sizeof nh, cudaMemcpyDeviceToHost, st);
+    if (have && e == cudaSuccess && nucl_counts) e = cudaMemcpyAsync(nh, nucl, sizeof nh, cudaMemcpyDeviceToHost, st);
     int64_t nr = 0;
-    if (e == cudaSuccess && !badh && nb > 0) {
+    const unsigned g2 = (unsigned)std::min<int64_t>((nb + 255) / 256, (int64_t)ctx->sm_count * 32);
+    if (have && e == cudaSuccess) {
         // run flags into A (no longer needed), scanned in place
-        const unsigned g2 = (unsigned)std::min<int64_t>((nb + 255) / 256, (int64_t)ctx->sm_count * 32);
         ingest_runflags_kernel<<<g2, 256, 0, st>>>(bseq, bpos, nb, A);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = device_scan<SumOp>(st, A, nb, scr);
-        if (e == cudaSuccess) {
-            ingest_runs_kernel<<<g2, 256, 0, st>>>(bseq, bpos, nb, A, d_run_start, d_run_seq, d_run_seqpos);
-            e = cudaGetLastError();
-        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(&nr, A + nb - 1, 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    if (have && e == cudaSuccess && resident) {
+        for (int k = 0; k < 3 && !rc; ++k)
+            rc = ensure(ctx, &ctx->d_srun[k], &ctx->cap_srun[k], (size_t)std::max<int64_t>(nr, 1));
+        d_run_start = ctx->d_srun[0];
+        d_run_seq = ctx->d_srun[1];
+        d_run_seqpos = ctx->d_srun[2];
+    }
+    if (have && e == cudaSuccess && !rc) {
+        ingest_runs_kernel<<<g2, 256, 0, st>>>(bseq, bpos, nb, A, d_run_start, d_run_seq, d_run_seqpos);
+        e = cudaGetLastError();
     }
     void *bufs[] = {A, B, Cc, D, sc0, scr, bad, bseq, bpos, nucl};
     for (void *b : bufs)
@@ -2147,6 +2179,7 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     if (e != cudaSuccess)
         return fail(ctx, e == cudaErrorMemoryAllocation ? BLAMM_ERR_NOMEM : BLAMM_ERR_CUDA, "FASTA ingest: %s",
                     cudaGetErrorString(e));
+    if (rc) return rc;
     if (badh) return fail(ctx, BLAMM_ERR_ARG, "Input file does not appear to be in fasta format");
     *n_bases = nb;
     *nruns = nr;
@@ -2154,6 +2187,101 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
     if (nucl_counts)
         for (int b = 0; b < 4; ++b) nucl_counts[b] = nh[b];
     return BLAMM_OK;
+}
+
+extern "C" {
+
+int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, char *d_bases, int64_t *n_bases,
+                             int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
+                             int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts)
+{
+    const NvtxRange nvtx_range("blamm_fasta_parse_device");
+    if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs) return BLAMM_ERR_ARG;
+    *n_bases = *nruns = *nseqs = 0;
+    if (nucl_counts)
+        for (int b = 0; b < 4; ++b) nucl_counts[b] = 0;
+    if (nraw == 0) return BLAMM_OK;
+    if (!d_raw || !d_bases || !d_run_start || !d_run_seq || !d_run_seqpos || !d_header_pos)
+        return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    return fasta_parse(ctx, d_raw, nraw, false, d_bases, d_run_start, d_run_seq, d_run_seqpos, d_header_pos,
+                       n_bases, nruns, nseqs, nucl_counts);
+}
+
+int blamm_stream_load_fasta(blamm_ctx *ctx, const char *raw, int64_t nraw, int64_t *n_bases, int64_t *nruns,
+                            int64_t *nseqs, uint64_t *nucl_counts)
+{
+    const NvtxRange nvtx_range("blamm_stream_load_fasta");
+    if (!ctx || nraw < 0 || !n_bases || !nruns || !nseqs || (nraw > 0 && !raw)) return BLAMM_ERR_ARG;
+    *n_bases = *nruns = *nseqs = 0;
+    if (nucl_counts)
+        for (int b = 0; b < 4; ++b) nucl_counts[b] = 0;
+    ctx->stream_n = ctx->stream_nruns = ctx->stream_nseqs = 0;
+    if (nraw == 0) return BLAMM_OK;
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure(ctx, &ctx->d_raw, &ctx->cap_raw, (size_t)nraw);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_raw, raw, (size_t)nraw, cudaMemcpyHostToDevice, ctx->stream));
+    rc = fasta_parse(ctx, ctx->d_raw, nraw, true, nullptr, nullptr, nullptr, nullptr, nullptr, n_bases, nruns,
+                     nseqs, nucl_counts);
+    if (rc) return rc;
+    ctx->stream_n = *n_bases;
+    ctx->stream_nruns = *nruns;
+    ctx->stream_nseqs = *nseqs;
+    return BLAMM_OK;
+}
+
+int blamm_stream_tables(blamm_ctx *ctx, int64_t *run_start, int64_t *run_seq, int64_t *run_seqpos,
+                        int64_t *header_pos)
+{
+    if (!ctx) return BLAMM_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int64_t *dst[4] = {run_start, run_seq, run_seqpos, header_pos};
+    const int64_t *src[4] = {ctx->d_srun[0], ctx->d_srun[1], ctx->d_srun[2], ctx->d_shdr};
+    const int64_t cnt[4] = {ctx->stream_nruns, ctx->stream_nruns, ctx->stream_nruns, ctx->stream_nseqs};
+    for (int k = 0; k < 4; ++k)
+        if (dst[k] && cnt[k] > 0)
+            CK(cudaMemcpyAsync(dst[k], src[k], 8 * (size_t)cnt[k], cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BLAMM_OK;
+}
+
+int blamm_scan_stream(blamm_ctx *ctx, int64_t begin, int64_t n, const int64_t *run_start, int64_t nruns,
+                      blamm_hit *hits, int64_t hit_cap, int64_t *n_hits)
+{
+    const NvtxRange nvtx_range("blamm_scan_stream");
+    if (!ctx || !n_hits || n < 0 || hit_cap < 0 || begin < 0) return BLAMM_ERR_ARG;
+    *n_hits = 0;
+    if (begin > ctx->stream_n || n > ctx->stream_n - begin)
+        return fail(ctx, BLAMM_ERR_ARG, "positions [%lld, %lld) outside the resident stream of %lld bases",
+                    (long long)begin, (long long)(begin + n), (long long)ctx->stream_n);
+    if (n == 0) return BLAMM_OK;
+    if (!run_start || nruns <= 0 || (hit_cap > 0 && !hits)) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    if (run_start[0] != 0) return fail(ctx, BLAMM_ERR_ARG, "run_start[0] must be 0");
+    for (int64_t r = 1; r < nruns; ++r)
+        if (run_start[r] <= run_start[r - 1] || run_start[r] >= n)
+            return fail(ctx, BLAMM_ERR_ARG, "run_start must ascend strictly inside [0, n)");
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "blamm_set_motifs was not called");
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    int rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, (size_t)nruns);
+    if (rc) return rc;
+    size_t hc = (size_t)ctx->hits_cap;
+    rc = ensure(ctx, &ctx->d_hits, &hc, (size_t)std::max<int64_t>(hit_cap, 1));
+    if (rc) return rc;
+    ctx->hits_cap = (int64_t)hc;
+    CK(cudaMemcpyAsync(ctx->d_runs, run_start, sizeof(int64_t) * nruns, cudaMemcpyHostToDevice, ctx->stream));
+    rc = scan_core(ctx, ctx->d_stream + begin, n, ctx->d_runs, nruns, ctx->d_hits, hit_cap, n_hits);
+    if (rc && rc != BLAMM_ERR_OVERFLOW) return rc;
+    const int64_t ncopy = std::min<int64_t>(*n_hits, hit_cap);
+    if (ncopy > 0)
+        CK(cudaMemcpyAsync(hits, ctx->d_hits, sizeof(blamm_hit) * ncopy, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]);
+    ctx->stats.total_ms = ms;
+    return rc;
 }
 
 }  // extern "C"

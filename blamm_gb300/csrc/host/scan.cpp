@@ -27,6 +27,7 @@
 #include "blamm_gpu.h"
 #include "format.h"
 #include "histogram.h"
+#include "ingest.h"
 #include "motif.h"
 #include "sequence.h"
 #include "species.h"
@@ -79,20 +80,25 @@ void check(blamm_ctx *ctx, int rc, const char *what)
         throw std::runtime_error(std::string("GPU error in ") + what + ": " + blamm_last_error(ctx));
 }
 
-// scan one chunk on one device, growing the hit buffer on overflow
-void scanChunk(Device &dev, const StreamChunk &chunk)
+// scan one chunk on one device, growing the hit buffer on overflow: the chunk's bases from
+// host memory, or (resident) positions [chunk.offset, chunk.offset + size) of the device's
+// resident stream
+void scanChunk(Device &dev, const StreamChunk &chunk, bool resident = false, int64_t size = 0)
 {
     const std::vector<int64_t> runs = chunk.runStarts();
     if (dev.hits.empty()) dev.hits.resize(1 << 20);
     while (true) {
         int64_t nh = 0;
-        const int rc = blamm_scan(dev.ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
-                                  (int64_t)runs.size(), dev.hits.data(), (int64_t)dev.hits.size(), &nh);
+        const int rc = resident
+            ? blamm_scan_stream(dev.ctx, chunk.offset, size, runs.data(), (int64_t)runs.size(), dev.hits.data(),
+                                (int64_t)dev.hits.size(), &nh)
+            : blamm_scan(dev.ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
+                         (int64_t)runs.size(), dev.hits.data(), (int64_t)dev.hits.size(), &nh);
         if (rc == BLAMM_ERR_OVERFLOW) {
             dev.hits.resize((size_t)(nh + nh / 8 + 1024));
             continue;
         }
-        check(dev.ctx, rc, "blamm_scan");
+        check(dev.ctx, rc, resident ? "blamm_scan_stream" : "blamm_scan");
         dev.hits.resize((size_t)nh);  // hits beyond nh were never written
         return;
     }
@@ -104,7 +110,7 @@ using Clock = std::chrono::steady_clock;
 // environment sets BLAMM_TIMING.
 struct PhaseTiming {
     std::mutex mu;
-    double s[5] = {0, 0, 0, 0, 0};
+    double s[6] = {0, 0, 0, 0, 0, 0};
     void add(int k, Clock::duration d)
     {
         std::lock_guard<std::mutex> lk(mu);
@@ -113,7 +119,8 @@ struct PhaseTiming {
     void report()
     {
         std::fprintf(stderr, "timing: GPU scan calls %.3f s, ordering hits %.3f s, formatting %.3f s, "
-                             "FASTA reading %.3f s, writing %.3f s\n", s[0], s[1], s[2], s[3], s[4]);
+                             "FASTA reading %.3f s (files %.3f s, GPU parsing %.3f s), writing %.3f s\n",
+                     s[0], s[1], s[2], s[3] + s[5], s[3], s[5], s[4]);
     }
 };
 PhaseTiming timing;
@@ -170,6 +177,187 @@ void formatHits(const std::vector<blamm_hit> &hits, size_t lo, size_t hi, const 
         std::memcpy(buf + k, mo.isRevCompl() ? "\t-\t.\t.\n" : "\t+\t.\t.\n", 7);
         out.append(buf, (size_t)k + 7);
     }
+}
+
+// A scanned chunk's occurrence lines: its own positions' hits in stream order, formatted
+// in parallel slices.  Adds the lines to *nlines.
+std::string chunkText(const Device &dev, const StreamChunk &chunk, const Species &sp,
+                      const MotifContainer &motifs, size_t numThreads, size_t *nlines)
+{
+    const auto t1 = Clock::now();
+    std::vector<blamm_hit> h = orderHits(dev.hits, chunk.payload, numThreads);
+    const auto t2 = Clock::now();
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(numThreads, h.size() / 20000 + 1));
+    std::vector<std::string> parts(nt);
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t)
+        th.emplace_back([&, t] { formatHits(h, h.size() * t / nt, h.size() * (t + 1) / nt, chunk, sp, motifs, parts[t]); });
+    for (auto &x : th) x.join();
+    std::string text;
+    size_t tl = 0;
+    for (auto &p : parts) tl += p.size();
+    text.reserve(tl);
+    for (auto &p : parts) text += p;
+    timing.add(1, t2 - t1);
+    timing.add(2, Clock::now() - t2);
+    *nlines += h.size();
+    return text;
+}
+
+// One species through the GPU FASTA reader: pieces of its text go to the devices'
+// resident streams (blamm_stream_load_fasta), each piece's chunks are scanned in place
+// (blamm_scan_stream) and formatted, and the text is written in (piece, chunk) order.
+// Returns the occurrences written.
+size_t scanSpeciesResident(std::vector<Device> &devs, const Species &sp, const MotifContainer &motifs,
+                           const Options &o, std::ostream &os)
+{
+    const int64_t overlap = (int64_t)motifs.maxMotifLen() - 1;
+    const char *env = std::getenv("BLAMM_CHUNK_BASES");
+    const int64_t payload = env ? std::max<int64_t>(1, std::atoll(env)) : (int64_t)1 << 26;
+    const int64_t maxFilt = (int64_t)sp.totalSeqLength();  // FastaBatch's _maxFiltSeqLen
+    FastaPieceReader rd(sp.sequenceFilenames(), ingestPieceBytes());
+    struct Out {
+        size_t nchunks = SIZE_MAX;
+        std::map<size_t, std::string> text;
+    };
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<std::pair<size_t, std::shared_ptr<std::string>>> todo;
+    std::map<size_t, Out> done;
+    // per piece: its first stream position and sequence index, known once the piece
+    // before it is loaded
+    std::vector<int64_t> baseStart{0}, seqStart{0};
+    size_t nextRead = 0, total = 0;
+    bool readerDone = false;
+    std::exception_ptr failure;
+    std::thread reader([&] {
+        try {
+            while (true) {
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return todo.size() < devs.size() + 1 || failure; });
+                    if (failure) break;
+                }
+                auto piece = std::make_shared<std::string>();
+                const auto t0 = Clock::now();
+                const bool more = rd.next(*piece);
+                timing.add(3, Clock::now() - t0);
+                if (!more) break;
+                std::lock_guard<std::mutex> lk(mu);
+                todo.emplace_back(nextRead++, std::move(piece));
+                cv.notify_all();
+            }
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(mu);
+            failure = std::current_exception();
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        readerDone = true;
+        cv.notify_all();
+    });
+    auto worker = [&](Device &dev) {
+        try {
+            while (true) {
+                std::pair<size_t, std::shared_ptr<std::string>> job;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return !todo.empty() || readerDone || failure; });
+                    if (failure || (todo.empty() && readerDone)) return;
+                    job = todo.front();
+                    todo.pop_front();
+                    cv.notify_all();
+                }
+                const size_t p = job.first;
+                const auto t0 = Clock::now();
+                int64_t nb = 0, nr = 0, ns = 0;
+                check(dev.ctx, blamm_stream_load_fasta(dev.ctx, job.second->data(), (int64_t)job.second->size(), &nb,
+                                                       &nr, &ns, nullptr),
+                      "blamm_stream_load_fasta");
+                job.second.reset();
+                std::vector<int64_t> rs((size_t)nr), rq((size_t)nr), rp((size_t)nr);
+                check(dev.ctx, blamm_stream_tables(dev.ctx, rs.data(), rq.data(), rp.data(), nullptr),
+                      "blamm_stream_tables");
+                timing.add(5, Clock::now() - t0);
+                int64_t b0 = 0, s0 = 0;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return baseStart.size() > p || failure; });
+                    if (failure) return;
+                    b0 = baseStart[p];
+                    s0 = seqStart[p];
+                    baseStart.push_back(b0 + nb);
+                    seqStart.push_back(s0 + ns);
+                    cv.notify_all();
+                }
+                nb = std::max<int64_t>(0, std::min<int64_t>(nb, maxFilt - b0));
+                size_t c = 0;
+                for (int64_t begin = 0; begin < nb; begin += payload, ++c) {
+                    const int64_t size = std::min<int64_t>(payload + overlap, nb - begin);
+                    StreamChunk chunk;
+                    residentChunk(rs, rq, rp, begin, size, std::min<int64_t>(payload, size), s0, chunk);
+                    const auto t1 = Clock::now();
+                    scanChunk(dev, chunk, true, size);
+                    timing.add(0, Clock::now() - t1);
+                    size_t lines = 0;
+                    std::string text = chunkText(dev, chunk, sp, motifs, o.numThreads, &lines);
+                    std::lock_guard<std::mutex> lk(mu);
+                    total += lines;
+                    done[p].text.emplace(c, std::move(text));
+                    cv.notify_all();
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                done[p].nchunks = c;
+                cv.notify_all();
+            }
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(mu);
+            failure = std::current_exception();
+            cv.notify_all();
+        }
+    };
+    std::vector<std::thread> workers;
+    for (auto &d : devs) workers.emplace_back(worker, std::ref(d));
+    // writer (this thread): pieces in order, each piece's chunks in order
+    size_t wp = 0, wc = 0;
+    while (true) {
+        std::string text;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            bool finished = false;
+            cv.wait(lk, [&] {
+                if (failure) return true;
+                auto it = done.find(wp);
+                if (it != done.end() && (it->second.text.count(wc) || it->second.nchunks == wc)) return true;
+                finished = readerDone && wp >= nextRead;
+                return finished;
+            });
+            if (failure || finished) break;
+            auto it = done.find(wp);
+            if (it->second.nchunks == wc) {  // this piece is written out
+                done.erase(it);
+                ++wp;
+                wc = 0;
+                continue;
+            }
+            auto t = it->second.text.find(wc);
+            text = std::move(t->second);
+            it->second.text.erase(t);
+            ++wc;
+        }
+        const auto t0 = Clock::now();
+        os << text;
+        timing.add(4, Clock::now() - t0);
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!failure && !(readerDone && wp >= nextRead))
+            failure = std::make_exception_ptr(std::runtime_error("writer stopped"));
+        cv.notify_all();
+    }
+    reader.join();
+    for (auto &w : workers) w.join();
+    if (failure) std::rethrow_exception(failure);
+    return total;
 }
 
 }  // namespace
@@ -339,7 +527,12 @@ int runScanModule(int argc, char **argv)
                                           (int)motifs.size(), lens.data(), thr.data()),
                   "blamm_set_motifs");
 
-        // reader -> per-device workers -> ordered writer
+        if (gpuFastaReader()) {
+            totMatches += scanSpeciesResident(devs, sp, motifs, o, os);
+            std::cout << "Progress... 100%  " << std::endl;
+            continue;
+        }
+        // host reader (BLAMM_FASTA_READER=host) -> per-device workers -> ordered writer
         FastaStream fs(sp.sequenceFilenames(), (int64_t)sp.totalSeqLength());
         const int64_t overlap = (int64_t)motifs.maxMotifLen() - 1;
         const char *env = std::getenv("BLAMM_CHUNK_BASES");
@@ -391,31 +584,12 @@ int runScanModule(int argc, char **argv)
                     const StreamChunk &chunk = *job.second;
                     const auto t0 = Clock::now();
                     scanChunk(dev, chunk);
-                    const auto t1 = Clock::now();
-                    // the chunk's own positions (the overlap belongs to the next chunk), in
-                    // stream order
-                    std::vector<blamm_hit> h = orderHits(dev.hits, chunk.payload, o.numThreads);
-                    const auto t2 = Clock::now();
-                    // format in parallel slices
-                    const size_t nt = std::max<size_t>(1, std::min<size_t>(o.numThreads, h.size() / 20000 + 1));
-                    std::vector<std::string> parts(nt);
-                    std::vector<std::thread> th;
-                    for (size_t t = 0; t < nt; ++t)
-                        th.emplace_back([&, t] {
-                            formatHits(h, h.size() * t / nt, h.size() * (t + 1) / nt, chunk, sp, motifs, parts[t]);
-                        });
-                    for (auto &x : th) x.join();
-                    std::string text;
-                    size_t tl = 0;
-                    for (auto &p : parts) tl += p.size();
-                    text.reserve(tl);
-                    for (auto &p : parts) text += p;
-                    const auto t3 = Clock::now();
-                    timing.add(0, t1 - t0);
-                    timing.add(1, t2 - t1);
-                    timing.add(2, t3 - t2);
+                    timing.add(0, Clock::now() - t0);
+                    // the chunk's own positions (the overlap belongs to the next chunk)
+                    size_t lines = 0;
+                    std::string text = chunkText(dev, chunk, sp, motifs, o.numThreads, &lines);
                     std::unique_lock<std::mutex> lk(mu);
-                    totMatches += h.size();
+                    totMatches += lines;
                     done.emplace(job.first, std::move(text));
                     cv.notify_all();
                 }

@@ -2,10 +2,13 @@
 #include "species.h"
 
 #include <fstream>
+#include <memory>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
 
+#include "blamm_gpu.h"
+#include "ingest.h"
 #include "sequence.h"
 
 namespace blamm {
@@ -13,6 +16,29 @@ namespace blamm {
 void Species::computeNucleotideComposition()
 {
     counts_ = {0, 0, 0, 0};
+    if (gpuFastaReader()) {
+        // the files' text parsed on the GPU piece by piece: counts and header names
+        blamm_ctx *ctx = nullptr;
+        if (blamm_ctx_create(0, &ctx) != BLAMM_OK)
+            throw std::runtime_error("no GPU for the FASTA reader (BLAMM_FASTA_READER=host reads on the host)");
+        std::unique_ptr<blamm_ctx, void (*)(blamm_ctx *)> guard(ctx, blamm_ctx_destroy);
+        FastaPieceReader rd(sequenceFilenames(), ingestPieceBytes());
+        std::string piece;
+        seqNames_.clear();
+        while (rd.next(piece)) {
+            int64_t nb = 0, nr = 0, ns = 0;
+            uint64_t c[4] = {0, 0, 0, 0};
+            if (blamm_stream_load_fasta(ctx, piece.data(), (int64_t)piece.size(), &nb, &nr, &ns, c) != BLAMM_OK)
+                throw std::runtime_error(blamm_last_error(ctx));
+            std::vector<int64_t> hp((size_t)ns);
+            if (blamm_stream_tables(ctx, nullptr, nullptr, nullptr, hp.data()) != BLAMM_OK)
+                throw std::runtime_error(blamm_last_error(ctx));
+            for (auto &n : headerNames(piece, hp)) seqNames_.push_back(std::move(n));
+            for (int b = 0; b < 4; ++b) counts_[(size_t)b] += c[b];
+        }
+        totLen_ = counts_[0] + counts_[1] + counts_[2] + counts_[3];
+        return;
+    }
     FastaStream fs(sequenceFilenames());
     StreamChunk chunk;
     while (fs.nextChunk(chunk, 1 << 24, 0)) {

@@ -84,7 +84,11 @@ struct TileDesc {
     int32_t g;        // k-steps of motif data: ceil(max motif length in the tile / 4)
     int32_t b_bytes;  // bytes of one B term: n x 16 x (g + 1) bf16 (last k-step: bias)
     int64_t b_off;    // byte offset of the tile's first B term in the B buffer
-    int64_t pad;
+    // 1: the tile's longest motif leaves motif positions 4g-2 and 4g-1 unused (length
+    // 4g-3 or 4g-2), so the bias pieces sit in K slots 8-10 of k-step g-1 and that
+    // k-step reads its second K core from the constant A rows: no bias MMA
+    int32_t fold;
+    int32_t pad;
 };
 
 struct TcParams {
@@ -240,12 +244,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     for (int i = threadIdx.x; i < CTL_WORDS; i += blockDim.x)
         if (i != CTL_TMEM) ctl[i] = 0;  // the TMEM word is written by the allocation below
     {
-        // constant A of the bias MMA: every row = [1, 1, 1, 0, ...] (16 K slots)
+        // constant A rows: 128 rows of 8 K slots [1, 1, 1, 0, ...], 16 B apart, then 128
+        // zero rows. With 8-row groups 128 B apart, the first block is a K core for any
+        // descriptor that points its second core there (LBO = block - start), and the bias
+        // MMA reads [ones | zeros] (start = block, LBO = 2048 B)
         uint4 *ab = reinterpret_cast<uint4 *>(smem + L.abias);
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) {  // 16 row groups x 2 cores x 8 rows
-            const int core = (i >> 3) & 1;
-            ab[i] = core == 0 ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
-        }
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            ab[i] = i < 128 ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
     }
     if (threadIdx.x == 0) {
         for (int s = 0; s < kEStages; ++s) {
@@ -282,11 +287,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         // Both walk every job of the CTA, so that both take part in every B tile change.
         const uint32_t mine = warp == kMmaWarp ? 0u : 1u;
         int cur_tile = -1;
-        uint32_t bphase = 0, idesc = 0, g_steps = 0, es = 0, eph = 0;
+        uint32_t bphase = 0, idesc = 0, g_steps = 0, es = 0, eph = 0, fold = 0;
         uint64_t bdesc_hi0 = 0, bdesc_lo0 = 0;  // k-step 0 of the current tile's B terms
         long long t_acc = 0, t_w = 0, t_b = 0;
         const long long t_start = tick<kProf>();
-        const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 128u, 256u);
+        const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 2048u, 128u);
         const uint64_t adesc_e = ptx::smem_desc(sbase + L.e0, 32u, 128u);
         const uint32_t e_step = (uint32_t)p.erows;  // one E stage in 16 B units
         uint32_t jc = 0;
@@ -307,6 +312,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 if (kProf) t_b += tick<kProf>() - tb;
                 const TileDesc td = s_tiles[tile];
                 g_steps = (uint32_t)td.g;
+                fold = (uint32_t)td.fold;
                 idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
                 const uint32_t sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
                 bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
@@ -329,16 +335,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 // term: the descriptors' address fields (bits 0-13, in 16 B units) advance by
                 // 4 and 16
                 const uint64_t adesc0 = adesc_e + es * e_step;
-                // D = -T (bias pieces in the last k-step of the hi term)
-                ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
-                if (kTerms == 2) {
-                    for (uint32_t g = 0; g < g_steps; ++g) {
-                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
-                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
-                    }
+                uint32_t acc = 1u, g_plain = g_steps;
+                if (fold) {
+                    g_plain = g_steps - 1u;  // the last k-step carries the bias
+                    acc = g_plain > 0u ? 1u : 0u;
                 } else {
-                    for (uint32_t g = 0; g < g_steps; ++g)
-                        ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, 1u);
+                    // D = -T (bias pieces in the extra k-step g of the hi term)
+                    ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
+                }
+                for (uint32_t g = 0; g < g_plain; ++g) {
+                    const uint32_t a = (g == 0u && fold) ? 0u : 1u;  // a folded tile starts at D = A B
+                    ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, a);
+                    if (kTerms == 2) ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
+                }
+                if (fold) {
+                    // k-step g-1: first K core = entries m0 + 4(g-1) + r, second K core = the
+                    // constant rows (the hi term's B holds the bias pieces there)
+                    const uint32_t a_last = sbase + L.e0 + es * e_step * 16u + 64u * g_plain;
+                    const uint64_t adesc_last = ptx::smem_desc(a_last, sbase + L.abias - a_last, 128u);
+                    ptx::mma_bf16(d_tmem, adesc_last, bdesc_hi0 + 16u * g_plain, idesc, acc);
+                    if (kTerms == 2) ptx::mma_bf16(d_tmem, adesc_last, bdesc_lo0 + 16u * g_plain, idesc, 1u);
                 }
                 ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
                 ptx::mma_commit(bars + 8 * (BAR_AFULL + s));

@@ -221,6 +221,33 @@ int blamm_fasta_parse_device(blamm_ctx *ctx, const char *d_raw, int64_t nraw, ch
                              int64_t *d_run_start, int64_t *d_run_seq, int64_t *d_run_seqpos, int64_t *nruns,
                              int64_t *d_header_pos, int64_t *nseqs, uint64_t *nucl_counts);
 
+/* The resident stream: FASTA text parsed on the device and kept in the context, so that
+ * the bases never pass through host memory between the file and the scan.
+ *
+ * blamm_stream_load_fasta: raw (host memory, nraw bytes: one or more files' text, each
+ * ending in a newline) is copied to the device and parsed as blamm_fasta_parse_device does
+ * (FastaBatch's filtered stream, src/sequence.cpp:142-293); the stream, its run table and
+ * the header offsets replace the context's previous resident stream.  *n_bases, *nruns,
+ * *nseqs and nucl_counts[4] (may be NULL) as blamm_fasta_parse_device returns them.
+ * Device memory: nraw + n_bases + 8 x (3 nruns + nseqs) bytes kept, plus ~56 bytes per raw
+ * byte during the call.  blamm_release_buffers drops the resident stream.
+ *
+ * blamm_stream_tables: the run table (stream position, sequence index, position inside
+ * the sequence; nruns entries each) and the header offsets (byte offset of each '>' in
+ * raw; nseqs entries) copied to host arrays; a NULL pointer skips that array.
+ *
+ * blamm_scan_stream: blamm_scan over positions [begin, begin + n) of the resident stream:
+ * run_start (host, nruns entries) relative to begin with run_start[0] == 0, hits (host)
+ * with positions relative to begin, BLAMM_ERR_OVERFLOW as blamm_scan.  The reference has
+ * no counterpart: its FastaBatch reads on the host (src/sequence.cpp:142-293) and each
+ * block's S is built on the host (src/sequence.cpp:299-340). */
+int blamm_stream_load_fasta(blamm_ctx *ctx, const char *raw, int64_t nraw, int64_t *n_bases, int64_t *nruns,
+                            int64_t *nseqs, uint64_t *nucl_counts);
+int blamm_stream_tables(blamm_ctx *ctx, int64_t *run_start, int64_t *run_seq, int64_t *run_seqpos,
+                        int64_t *header_pos);
+int blamm_scan_stream(blamm_ctx *ctx, int64_t begin, int64_t n, const int64_t *run_start, int64_t nruns,
+                      blamm_hit *hits, int64_t hit_cap, int64_t *n_hits);
+
 /* Number of CUDA devices (0 when there is no driver or device). */
 int blamm_device_count(int *n);
 

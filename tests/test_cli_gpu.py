@@ -58,3 +58,43 @@ def test_cli_motifs_longer_than_the_tensor_core_limit(tmp_path):
         outs[name] = sorted(open(d / "occurrences.txt").read().splitlines())
     assert len(outs["ours"]) > 0 and outs["ours"] == outs["oracle"]
     assert any("LONG300" in line for line in outs["ours"])
+
+
+@pytest.mark.parametrize("kind,arg", [("edge", False), ("edge", True), ("random", 0), ("random", 1)])
+@pytest.mark.parametrize("piece", ["1", "268435456"])
+def test_gpu_and_host_fasta_readers_write_the_same_files(tmp_path, kind, arg, piece):
+    """The default FASTA reader (the text parsed on the GPU in pieces cut at header lines,
+    kept on the device and scanned there) and the host reader (FastaStream, which the CPU
+    suite pins to the reference's `dict` output on these cases) write byte-identical .dict,
+    hist, PWMthresholds.txt and occurrence files.  Pieces of 1 byte put every sequence in a
+    piece of its own; chunks of 5000 bases cut the pieces further."""
+    import os
+    import subprocess
+
+    from fresh_cases import edge_case, random_case
+    make = edge_case if kind == "edge" else random_case
+    outs = {}
+    for name, env in (("host", {"BLAMM_FASTA_READER": "host"}),
+                      ("gpu", {"BLAMM_INGEST_PIECE_BYTES": piece, "BLAMM_CHUNK_BASES": "5000"})):
+        d = tmp_path / name
+        d.mkdir()
+        for cmd in make(d, arg):
+            r = subprocess.run([CLI_PATH] + cmd, cwd=d, capture_output=True, text=True,
+                               env=dict(os.environ, **env))
+            assert r.returncode == 0, (name, cmd, r.stderr[-800:])
+        outs[name] = d
+    files = sorted(p.name for p in outs["host"].iterdir() if p.is_file())
+    assert "sequences.mf.dict" in files and any(f.startswith("occ_") for f in files)
+    for f in files:
+        assert (outs["host"] / f).read_bytes() == (outs["gpu"] / f).read_bytes(), f
+
+
+def test_gpu_reader_rejects_sequence_data_before_a_header(tmp_path):
+    """The GPU reader stops like the reference's dict module (FastaBatch::getNextLine throws,
+    blstools.cpp:93-101 exits 1)."""
+    import subprocess
+    (tmp_path / "bad.fa").write_text("ACGT\n>s1\nACGTACGT\n")
+    (tmp_path / "bad.mf").write_text("sp\tbad.fa\n")
+    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=tmp_path, capture_output=True)
+    assert r.returncode == 1
+    assert b"Input file does not appear to be in fasta format" in r.stderr + r.stdout

@@ -95,3 +95,76 @@ def test_nucleotide_counts_equal_the_reference_dictionary(scanner, tmp_path):
     fa.write_bytes(gzip.open(os.path.join(d, "seqs", "seqs.fa.gz")).read())
     got = _gpu_parse(scanner, _concat([str(fa)]))
     assert [int(x) for x in got[5]] == want
+
+
+def _random_fasta(tmp_path, seed: int, nfiles: int = 3, maxlen: int = 20_000):
+    rng = np.random.default_rng(seed)
+    files = []
+    for fi in range(nfiles):
+        lines = []
+        for si in range(int(rng.integers(1, 6))):
+            lines.append(f">seq{fi}_{si} description")
+            L = int(rng.integers(0, maxlen))
+            s = rng.choice(np.frombuffer(b"ACGTACGTacgtNNnRY", dtype=np.uint8), size=L)
+            for _ in range(int(rng.integers(0, 4))):
+                a = int(rng.integers(0, max(1, L)))
+                s[a:a + int(rng.integers(1, 500))] = ord("N")
+            w = int(rng.integers(1, 120))
+            for k in range(0, L, w):
+                lines.append(s[k:k + w].tobytes().decode())
+        p = tmp_path / f"r{seed}_{fi}.fa"
+        p.write_bytes(("\n".join(lines) + "\n").encode())
+        files.append(str(p))
+    return files
+
+
+def _chunk_runs(run_start, begin, size):
+    """The run starts inside [begin, begin + size), relative to begin, led by the run in
+    effect at begin (FastaStream::nextChunk's markers)."""
+    k = int(np.searchsorted(run_start, begin, side="right")) - 1
+    inner = run_start[(run_start > begin) & (run_start < begin + size)] - begin
+    return np.concatenate([[0], inner]).astype(np.int64) if k >= 0 else inner
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_resident_stream_equals_the_oracle_stream_and_scans_in_chunks(scanner, tmp_path, seed):
+    """blamm_stream_load_fasta keeps FastaBatch's stream on the device: its run table equals the
+    oracle's, and blamm_scan_stream over overlapping chunks of it gives the whole stream's hits."""
+    import oracle
+    from bankutil import make_bank, same_hits
+    files = _random_fasta(tmp_path, seed)
+    raw = _concat(files)
+    nb, nr, ns, nucl = scanner.stream_load_fasta(raw)
+    bases, run_start, run_seq, run_seqpos = _oracle_stream(files)
+    rs, rq, rp, hp = scanner.stream_tables()
+    assert nb == len(bases) and nr == len(run_start) and ns == raw.count(b"\n>") + raw.startswith(b">")
+    assert np.array_equal(rs, run_start) and np.array_equal(rq, run_seq) and np.array_equal(rp, run_seqpos)
+    assert all(raw[int(p)] == ord(">") for p in hp)
+    low = bases | 0x20
+    assert [int(x) for x in nucl] == [int(np.count_nonzero(low == ord(c))) for c in "acgt"]
+    P, lens, thr = make_bank(60 + seed, 24, 5, 20, rel=0.8)
+    scanner.set_mode("auto")
+    scanner.set_motifs(P, lens, thr)
+    whole = oracle.scan(bases, run_start, P, lens, thr)
+    payload, overlap = 7_001, int(lens.max()) - 1
+    parts = []
+    for begin in range(0, nb, payload):
+        size = min(payload + overlap, nb - begin)
+        h = scanner.scan_stream(begin, size, _chunk_runs(run_start, begin, size))
+        h = h[h["pos"] < payload]
+        h["pos"] += begin
+        parts.append(h)
+    ok, msg = same_hits(np.concatenate(parts), whole)
+    assert ok, msg
+    assert len(whole) > 100
+
+
+def test_resident_stream_rejects_positions_outside_it(scanner):
+    from blamm_gb300 import BlammError
+    from bankutil import make_bank
+    scanner.stream_load_fasta(b">s\nACGTACGTAC\n")
+    P, lens, thr = make_bank(5, 2, 3, 4)
+    scanner.set_motifs(P, lens, thr)
+    with pytest.raises(BlammError):
+        scanner.scan_stream(4, 7, np.zeros(1, dtype=np.int64))
+    assert len(scanner.scan_stream(4, 6, np.zeros(1, dtype=np.int64), hit_cap=1000)) >= 0

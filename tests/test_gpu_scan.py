@@ -30,6 +30,29 @@ def test_tensor_core_sums_are_exact(scanner, mode):
     assert bad.size == 0, f"{bad.size} mismatches, first {D.ravel()[bad[0]]} vs {want.ravel()[bad[0]]}"
 
 
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+@pytest.mark.parametrize("lengths", [(1, 2), (3, 4), (5, 6), (7, 8), (1, 10), (13, 14), (29, 30)])
+def test_bias_in_the_last_k_step(scanner, mode, lengths):
+    """A tile whose longest motif has length 4g-3 or 4g-2 carries the threshold bias in the
+    second K core of its last k-step (no bias MMA); (3, 4), (7, 8) keep the bias MMA. Both
+    give the exact sums and the oracle's hits, with some thresholds below every score."""
+    lo, hi = lengths
+    P, lens, thr = make_bank(100 + lo, 24, lo, hi, rel=0.9)
+    thr[::5] = np.float32(-1e3)  # every window of those columns is a hit
+    bases, runs = make_stream(200 + lo, 8000, nruns=3, lower_frac=0.05)
+    scanner.set_mode(mode)
+    scanner.set_motifs(P, lens, thr)
+    p0, npos = 40, 600
+    D = scanner.debug_scores(bases, p0, npos)
+    Q = quantized_columns(P, lens, 2 if mode == "bf16x2" else 1)
+    want = exact_window_scores(bases, Q, lens, p0, npos)
+    bad = np.flatnonzero(D.astype(np.float64).ravel() != want.ravel())
+    assert bad.size == 0, f"{bad.size} mismatches, first {D.ravel()[bad[0]]} vs {want.ravel()[bad[0]]}"
+    got = scanner.scan(bases, runs, hit_cap=None)
+    ok, msg = same_hits(got, oracle.scan(bases, runs, P, lens, thr))
+    assert ok, msg
+
+
 @pytest.mark.parametrize("mode", MODES)
 def test_scan_matches_oracle(scanner, mode):
     P, lens, thr = make_bank(3, 64, 5, 30, rel=0.88)

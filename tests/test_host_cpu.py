@@ -13,13 +13,17 @@ from blamm_gb300 import workloads
 from blamm_gb300._native import CLI_PATH, FastaReader, MotifBank
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# the command line without a GPU: its host FASTA reader (the default reader parses on the GPU)
+HOST_READER = {"BLAMM_FASTA_READER": "host"}
+HOST_ENV = dict(os.environ, **HOST_READER)
 
 
 @pytest.mark.parametrize("case", gc.CASES)
 def test_cli_dict_and_hist_match_reference(tmp_path, case):
     spec = gc.load(case)
     d = gc.stage(case, str(tmp_path))
-    gc.run(CLI_PATH, d, spec, skip=[lambda c: c[0] == "scan", lambda c: c[0] == "hist" and "-e" in c])
+    gc.run(CLI_PATH, d, spec, skip=[lambda c: c[0] == "scan", lambda c: c[0] == "hist" and "-e" in c],
+           env=HOST_READER)
     gc.compare(d, case, spec, what=("dict", "hist"))
 
 
@@ -125,7 +129,7 @@ def test_cli_dict_and_hist_match_reference_on_fresh_cases(tmp_path, kind, arg):
         cmds = [c for c in make(d, arg) if c[0] != "scan"]
         for cmd in cmds:
             subprocess.run([binary] + cmd, cwd=d, check=True, stdout=subprocess.DEVNULL,
-                           env=dict(os.environ, OPENBLAS_NUM_THREADS="1"))
+                           env=dict(HOST_ENV, OPENBLAS_NUM_THREADS="1"))
         outs[name] = d
     files = ["sequences.mf.dict"] + sorted(p.name for p in outs["ref"].glob("hist_*"))
     assert len(files) > 1
@@ -211,7 +215,7 @@ def test_cli_errors_match_reference_behaviour(tmp_path):
     """Host-side failures: missing files give a message and EXIT_FAILURE like the reference."""
     import subprocess
     d = gc.stage("cb", str(tmp_path))
-    r = subprocess.run([CLI_PATH, "dict", "missing.mf"], cwd=d, capture_output=True)
+    r = subprocess.run([CLI_PATH, "dict", "missing.mf"], cwd=d, capture_output=True, env=HOST_ENV)
     assert r.returncode == 1 and b"Could not open file: missing.mf" in r.stderr
     r = subprocess.run([CLI_PATH, "hist", "motifs.cb", "sequences.mf"], cwd=d, capture_output=True)
     assert r.returncode == 1 and b"Cannot open file: sequences.mf.dict" in r.stderr
@@ -224,7 +228,7 @@ def test_cli_errors_match_reference_behaviour(tmp_path):
         f.write("ACGT\n>x\nACGT\n")
     with open(os.path.join(d, "bad.mf"), "w") as f:
         f.write("sp\tbad.fa\n")
-    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=d, capture_output=True)
+    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=d, capture_output=True, env=HOST_ENV)
     assert r.returncode == 1 and b"does not appear to be in fasta format" in r.stderr
 
 
@@ -250,7 +254,7 @@ def test_cli_rejects_sequence_data_before_a_header(tmp_path):
     import subprocess
     (tmp_path / "bad.fa").write_text("ACGT\n>s1\nACGTACGT\n")
     (tmp_path / "bad.mf").write_text("sp\tbad.fa\n")
-    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=tmp_path, capture_output=True)
+    r = subprocess.run([CLI_PATH, "dict", "bad.mf"], cwd=tmp_path, capture_output=True, env=HOST_ENV)
     assert r.returncode == 1
     assert b"Input file does not appear to be in fasta format" in r.stderr + r.stdout
 
