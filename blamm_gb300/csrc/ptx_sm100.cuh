@@ -72,6 +72,38 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
     }
 }
 
+// try_wait without a suspend-time hint: the hardware's own time limit.  The drain warps
+// wait this way for a full accumulator (with the 20 us hint they resumed measurably later).
+__device__ __forceinline__ bool mbar_try_wait_nohint(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_nohint(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                                 long long limit_cycles)
+{
+    if (mbar_try_wait_nohint(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try_wait_nohint(bar, parity)) return true;
+        if ((it & 7u) == 0) {
+            if (*abort_flag) return false;
+            if (clock64() - t0 > limit_cycles) {
+                *abort_flag = 1;
+                return false;
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
@@ -185,24 +217,31 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, one MMA of M x N x 16, issued by one thread.
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate)
+// D[tmem] (+)= A[smem] * B[smem]^T, one MMA of M x N x 16, issued by the one lane that
+// elect.sync picks in a converged warp: the warp runs the issuing loop together, so the
+// descriptors are warp-uniform values.  (The same loop run by one lane alone issued
+// measurably slower.)
+__device__ __forceinline__ void mma_bf16_elect(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                               uint32_t idesc, uint32_t accumulate)
 {
     asm volatile(
-        "{\n\t.reg .pred p;\n\t"
+        "{\n\t.reg .pred p, e;\n\t"
+        "elect.sync _|e, 0xffffffff;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
-// Arrive once on an mbarrier when every tcgen05 op issued so far by this
-// thread has completed.
-__device__ __forceinline__ void mma_commit(uint32_t bar)
+// Arrive once on an mbarrier when every tcgen05 op issued so far by the issuing thread has
+// completed; issued by the lane that elect.sync picks (one arrival per warp).
+__device__ __forceinline__ void mma_commit_elect(uint32_t bar)
 {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
+    asm volatile(
+        "{\n\t.reg .pred e;\n\t"
+        "elect.sync _|e, 0xffffffff;\n\t"
+        "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(bar)
+        : "memory");
 }
 
 // 32 lanes x 32 consecutive 32-bit columns: thread t of the warp receives the

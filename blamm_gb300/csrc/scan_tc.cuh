@@ -282,9 +282,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
     const int njobs = p.ntiles * (int)p.n_mtiles;  // < 2^31 (host-checked)
     const int n_mt = (int)p.n_mtiles;
 
-    if ((warp == kMmaWarp || warp == kMmaWarp2) && lane == 0) {
+    if (warp == kMmaWarp || warp == kMmaWarp2) {
         // ============ MMA issuers: warp 16 the even jobs, warp 17 the odd ones ============
         // Both walk every job of the CTA, so that both take part in every B tile change.
+        // The whole warp runs the loop (warp-uniform descriptors, one vote per wait); one
+        // elected lane issues each MMA and commit.
         const uint32_t mine = warp == kMmaWarp ? 0u : 1u;
         int cur_tile = -1;
         uint32_t bphase = 0, idesc = 0, g_steps = 0, es = 0, eph = 0, fold = 0;
@@ -297,14 +299,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         uint32_t jc = 0;
         bool ok = true;
         if (p.debug_stall) ok = ptx::mbar_wait(bars + 8 * BAR_NEVER, 0, s_abort, p.wait_limit);
+        ok = __all_sync(0xffffffffu, ok);
         JobIter it;
         for (it.init(blockIdx.x, n_mt); it.job < njobs && ok; it.next(gridDim.x, n_mt), ++jc) {
             const int tile = it.tile;
             if (tile != cur_tile) {
                 const long long tb = tick<kProf>();
                 // this issuer is done with the old tile once its MMAs so far are complete
-                if (cur_tile >= 0) ptx::mma_commit(bars + 8 * BAR_TILE);
-                ok = ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit);
+                if (cur_tile >= 0) ptx::mma_commit_elect(bars + 8 * BAR_TILE);
+                ok = __all_sync(0xffffffffu, ptx::mbar_wait(bars + 8 * BAR_BFULL, bphase, s_abort, p.wait_limit));
                 bphase ^= 1;
                 if (!ok) break;
                 ptx::tc_fence_after();
@@ -324,6 +327,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 ok = ptx::mbar_wait_spin(bars + 8 * (BAR_AEMPTY + s), ph ^ 1u, s_abort, p.wait_limit);
                 const long long t1 = tick<kProf>();
                 ok = ok && ptx::mbar_wait_spin(bars + 8 * (BAR_WFULL + es), eph, s_abort, p.wait_limit);
+                ok = __all_sync(0xffffffffu, ok);
                 if (kProf) {
                     t_acc += t1 - t0;
                     t_w += tick<kProf>() - t1;
@@ -341,23 +345,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     acc = g_plain > 0u ? 1u : 0u;
                 } else {
                     // D = -T (bias pieces in the extra k-step g of the hi term)
-                    ptx::mma_bf16(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
+                    ptx::mma_bf16_elect(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
                 }
                 for (uint32_t g = 0; g < g_plain; ++g) {
                     const uint32_t a = (g == 0u && fold) ? 0u : 1u;  // a folded tile starts at D = A B
-                    ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, a);
-                    if (kTerms == 2) ptx::mma_bf16(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
+                    ptx::mma_bf16_elect(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, a);
+                    if (kTerms == 2) ptx::mma_bf16_elect(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
                 }
                 if (fold) {
                     // k-step g-1: first K core = entries m0 + 4(g-1) + r, second K core = the
                     // constant rows (the hi term's B holds the bias pieces there)
                     const uint32_t a_last = sbase + L.e0 + es * e_step * 16u + 64u * g_plain;
                     const uint64_t adesc_last = ptx::smem_desc(a_last, sbase + L.abias - a_last, 128u);
-                    ptx::mma_bf16(d_tmem, adesc_last, bdesc_hi0 + 16u * g_plain, idesc, acc);
-                    if (kTerms == 2) ptx::mma_bf16(d_tmem, adesc_last, bdesc_lo0 + 16u * g_plain, idesc, 1u);
+                    ptx::mma_bf16_elect(d_tmem, adesc_last, bdesc_hi0 + 16u * g_plain, idesc, acc);
+                    if (kTerms == 2) ptx::mma_bf16_elect(d_tmem, adesc_last, bdesc_lo0 + 16u * g_plain, idesc, 1u);
                 }
-                ptx::mma_commit(bars + 8 * (BAR_WEMPTY + es));
-                ptx::mma_commit(bars + 8 * (BAR_AFULL + s));
+                ptx::mma_commit_elect(bars + 8 * (BAR_WEMPTY + es));
+                ptx::mma_commit_elect(bars + 8 * (BAR_AFULL + s));
             }
             if (++es == (uint32_t)kEStages) {
                 es = 0;
@@ -365,9 +369,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             }
         }
         // drain: nothing may still write TMEM or shared memory when they are freed
-        ptx::mma_commit(bars + 8 * (BAR_DRAIN + mine));
+        ptx::mma_commit_elect(bars + 8 * (BAR_DRAIN + mine));
         if (!ptx::mbar_wait_drain(bars + 8 * (BAR_DRAIN + mine), 0, p.wait_limit)) *s_abort = 1;
-        if (kProf) {
+        if (kProf && lane == 0) {
             long long *pr = p.prof + 32 * blockIdx.x;
             pr[mine] += t_acc;
             if (mine == 0) {
@@ -467,7 +471,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
             const int slot0 = s_tiles[tile].slot0, nch = s_tiles[tile].n >> 5;
             const uint32_t s = jc & acc_mask, ph = (jc >> acc_shift) & 1u;
             const long long t0 = tick<kProf>();
-            if (!ptx::mbar_wait(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
+            if (!ptx::mbar_wait_nohint(bars + 8 * (BAR_AFULL + s), ph, s_abort, p.wait_limit)) break;
             const long long t1 = tick<kProf>();
             if (kProf) t_af += t1 - t0;
             ptx::tc_fence_after();
