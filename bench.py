@@ -48,7 +48,7 @@ def args_parse():
     ap.add_argument("--no-modes", action="store_true", help="skip the bf16 / fp32 comparison runs")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-cli", action="store_true", help="skip the end-to-end command-line measurement")
-    ap.add_argument("--mode", default="auto", choices=["auto", "bf16", "bf16x2"],
+    ap.add_argument("--mode", default="auto", choices=["auto", "bf16", "bf16x2", "e4m3"],
                     help="headline arithmetic: auto (the library default, autotuned on a sample) or a fixed "
                          "term count with the default tile plan (no autotuner launches, for profiling)")
     ap.add_argument("--serve-requests", type=int, default=48, help="distinct requests of the serving pool")
@@ -440,7 +440,8 @@ def emitted_score_error(hits, ref, npos: int) -> dict:
 
 def precision_other_configs(seed: int, npos: int = 2048) -> dict:
     """Score error against FP64 on the other cases' shapes, each on a sample generated like the
-    case itself: the raw tensor-core sums (one and two BF16 terms) and the emitted scores."""
+    case itself: the raw tensor-core sums (one and two BF16 terms, one E4M3 term) and the emitted
+    scores."""
     from blamm_gb300 import GpuScanner, workloads
     from blamm_gb300._native import MotifBank
     rng = np.random.default_rng([seed, 9])
@@ -465,7 +466,7 @@ def precision_other_configs(seed: int, npos: int = 2048) -> dict:
         thr = bank.pvalue_thresholds(bgp, pv)
         ref = fp64_window_scores(bases, P, lens, npos)
         res = {}
-        for mode in ("bf16x2", "bf16"):
+        for mode in ("bf16x2", "bf16", "e4m3"):
             sc = GpuScanner(0, mode)
             sc.set_motifs(P, lens, thr)
             res["mma_" + mode] = mma_score_error(sc, bases, P, lens, ref, npos)
@@ -573,7 +574,7 @@ def _device_scan(sc, torch, d_b, n, d_r, nr, cap):
 def run_genome_1gbp(a):
     """2000 motifs (4000 columns) over 1 Gbp (2nd-order Markov, GC 0.41, 1 % N runs),
     p = 1e-4 and 1e-5 thresholds inverted in FP64 on the GPU; BF16 split vs single-term BF16
-    (same hits required); the plain FP32 form on a 100 Mbp sample."""
+    vs one E4M3 term (same hits required); the plain FP32 form on a 100 Mbp sample."""
     import torch
     from blamm_gb300 import GpuScanner, HIT_DTYPE, workloads
     t0 = time.perf_counter()
@@ -593,7 +594,7 @@ def run_genome_1gbp(a):
         sc.set_motifs(P, lens, thr[pi])
         res = {"pvalue": pv}
         digests = {}
-        for mode in ("bf16x2", "bf16"):
+        for mode in ("bf16x2", "bf16", "e4m3"):
             sc.set_mode(mode)
             from blamm_gb300 import HIT_DTYPE as HD
             nh = sc.scan_device(d_b.data_ptr(), n, d_r.data_ptr(), len(runs), 0, 0, overflow_ok=True)
@@ -621,6 +622,7 @@ def run_genome_1gbp(a):
                          "tiles": int(st["tiles"])}
             del d_h
         res["same_hits_bf16_vs_bf16x2"] = digests["bf16"] == digests["bf16x2"]
+        res["same_hits_e4m3_vs_bf16x2"] = digests["e4m3"] == digests["bf16x2"]
         out["runs"].append(res)
     # plain FP32 form on a 100 Mbp sample of the same stream, same hits as the split there
     m = min(n, 100_000_000)
@@ -846,7 +848,7 @@ def run_ours(a, rank, world, local):
         # headline's term count)
         keep_plan = sc.plan_options()
         sc.set_plan_options(256, 700.0)
-        for mode in ("bf16x2", "bf16", "fp32"):
+        for mode in ("bf16x2", "bf16", "e4m3", "fp32"):
             sc.set_mode(mode)
             device_steps(1, False)
             mms, msc, _, mnh = device_steps(max(1, min(3, a.steps)), True)
@@ -863,7 +865,7 @@ def run_ours(a, rank, world, local):
     if rank == 0:
         npos = 2048
         ref = fp64_window_scores(bases[:npos + 256], P, lens, npos)
-        for mode in ("bf16x2", "bf16"):
+        for mode in ("bf16x2", "bf16", "e4m3"):
             sc.set_mode(mode)
             precision["mma_" + mode] = mma_score_error(sc, bases, P, lens, ref, npos)
         sc.set_mode(a.mode)
@@ -882,9 +884,10 @@ def run_ours(a, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": ("bf16x2 (hi+lo fixed-point split" if terms == 2 else "bf16 (one fixed-point term")
+        "dtype": ({2: "bf16x2 (hi+lo fixed-point split", 8: "e4m3 (one E4M3 term of P x 2^k"}
+                  .get(terms, "bf16 (one fixed-point term"))
                  + ", fp32 accumulate) + fp32 rescoring"
-                 + ("; term count autotuned" if a.mode == "auto" else ""),
+                 + ("; form autotuned" if a.mode == "auto" else ""),
         "data": "synthetic (seeded numpy; the 100 Mbp x 512-motif shapes)",
         "config": {"workload": "genome_100mbp: 512 motifs (1024 columns, L 5-30, both strands, Dirichlet(0.5) "
                                "columns of 100 counts) x 24 iid sequences (A=T=0.29) log-uniform 1-20 Mbp, "
@@ -909,9 +912,11 @@ def run_ours(a, rank, world, local):
                      "scan_launches_per_step": scan_launches,
                      "note": f"algorithmic flops = 8 * sum(L) = {flops_per_bp:.0f} per bp over {n} bp in "
                              f"{scan_launches} window launch(es) per step, divided by their summed time; "
-                             f"traffic per launch ({n / scan_launches:.0f} positions); {terms} BF16 term(s) "
-                             f"issue {terms} MMA(s) per flop (ceiling {1 / terms:g} before padding and the "
-                             f"bias MMA); peak {peak_src}"},
+                             f"traffic per launch ({n / scan_launches:.0f} positions); "
+                             + (f"{terms} BF16 term(s) issue {terms} MMA(s) per flop (ceiling {1 / terms:g} "
+                                if terms in (1, 2) else "one E4M3 term: half the BF16 MMA instructions per flop "
+                                "at twice the BF16 rate (ceiling 2 of the BF16 peak ")
+                             + f"before padding and the bias MMA); peak {peak_src}"},
         "modes": modes,
         "score_error_vs_fp64": precision,
         "clocks": clk,

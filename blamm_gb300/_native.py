@@ -21,7 +21,7 @@ BLAMM_ERR_NOMEM = -5
 BLAMM_ERR_UNSUPPORTED = -6
 BLAMM_ERR_STATE = -7
 
-MODES = {"fp32": 0, "bf16": 1, "bf16x2": 2, "auto": 3}
+MODES = {"fp32": 0, "bf16": 1, "bf16x2": 2, "auto": 3, "e4m3": 4}
 
 HIT_DTYPE = np.dtype([("pos", "<i8"), ("col", "<i4"), ("score", "<f4")])
 

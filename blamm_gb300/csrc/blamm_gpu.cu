@@ -52,7 +52,7 @@ struct blamm_ctx {
     cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::string err;
     int mode = BLAMM_MODE_AUTO;
-    int auto_terms = 1;  // BLAMM_MODE_AUTO: BF16 terms in use (1 until the autotuner measured both)
+    int auto_terms = 1;  // BLAMM_MODE_AUTO: the form in use, 1 or 2 BF16 terms or kE4M3 (1 until tuned)
     bool plain_timed = false, rescore_timed = false;
     int lower_scores = 0;  // soft-masked bases add their PWM value (simple scan) when 1
     long long wait_limit = 4000000000LL;  // clock64 cycles (about 2 s)
@@ -92,6 +92,7 @@ struct blamm_ctx {
     std::vector<double> colq_guard;
     std::vector<uint32_t> colq_off;  // column c's 4L values start at colq_off[c]
     std::vector<uint16_t> colq_hi, colq_lo;
+    std::vector<uint8_t> colq_e8;  // E4M3 codes of P(c) x 2^colq_k[c] (the E4M3 form)
     // planner knobs (the autotuner sets them): widest N tile, fixed cycles per job
     int plan_nmax = 256;
     double plan_job_cost = 700.0;
@@ -221,6 +222,69 @@ inline uint16_t bf16_bits_exact(double v)
 // 4g-1 (the second K core of its last k-step) unused: the bias rides there.
 inline bool bias_folds(int L) { return L % 4 == 1 || L % 4 == 2; }
 
+// E4M3 (sign, 4 exponent bits with bias 7, 3 mantissa bits; exponent 0 subnormal, largest
+// finite 448).  In units of 2^-9 every E4M3 value is an integer: m (subnormal, m < 8) or
+// (8 + m) 2^(e-1).
+constexpr int64_t kE4M3MaxUnits = 448 * 512;
+
+// The E4M3 value nearest to v (ties to even mantissa), as its code; |v| <= 448.
+inline uint8_t e4m3_round(double v)
+{
+    const uint8_t sign = v < 0 ? 0x80 : 0;
+    const double a = std::fabs(v) * 512.0;  // in units of 2^-9
+    if (a < 7.5) {  // subnormal: nearest integer, 8 rounds up to the smallest normal
+        const double r = std::nearbyint(a);
+        return (uint8_t)(sign | (r >= 8.0 ? 0x08 : (uint8_t)r));
+    }
+    int e = 1;
+    while (e < 15 && a >= 16.0 * std::ldexp(1.0, e - 1)) ++e;  // (8+m) 2^(e-1) with m < 8
+    double m = std::nearbyint(a / std::ldexp(1.0, e - 1)) - 8.0;  // ties to even (FE_TONEAREST)
+    if (m >= 8.0) {  // carried into the next binade
+        m = 0.0;
+        ++e;
+    }
+    if (e > 15 || (e == 15 && m > 6.0)) {  // beyond 448 (callers keep |v| <= 256)
+        e = 15;
+        m = 6.0;
+    }
+    return (uint8_t)(sign | (uint8_t)(e << 3) | (uint8_t)m);
+}
+
+// value of an E4M3 code in units of 2^-9
+inline int64_t e4m3_units(uint8_t code)
+{
+    const int e = (code >> 3) & 15, m = code & 7;
+    const int64_t a = e == 0 ? m : (int64_t)(8 + m) << (e - 1);
+    return code & 0x80 ? -a : a;
+}
+
+// Split an integer number of 2^-9 units into E4M3 values that add up to it exactly, the
+// largest first (each step leaves less than an eighth of the rest).  Returns the count,
+// or -1 if more than `cap` pieces would be needed.
+inline int e4m3_pieces(int64_t t, uint8_t *out, int cap)
+{
+    int n = 0;
+    while (t != 0) {
+        if (n == cap) return -1;
+        const int64_t a = t < 0 ? -t : t;
+        uint8_t code;
+        if (a >= kE4M3MaxUnits) {
+            code = 0x7E;  // 448
+        } else if (a < 8) {
+            code = (uint8_t)a;
+        } else {
+            int e = 1;
+            while (e < 15 && a >= ((int64_t)16 << (e - 1))) ++e;
+            const int64_t m = (a >> (e - 1)) - 8;  // rounded down: the piece never exceeds a
+            code = (uint8_t)((e << 3) | (int)m);
+        }
+        if (t < 0) code |= 0x80;
+        out[n++] = code;
+        t -= e4m3_units(code);
+    }
+    return n;
+}
+
 }  // namespace
 
 static int build_plan(blamm_ctx *ctx, int terms)
@@ -241,12 +305,18 @@ static int build_plan(blamm_ctx *ctx, int terms)
                     "motif length %d exceeds the tensor-core limit %d (use BLAMM_MODE_FP32)", lmax_sel,
                     kMaxTcLen);
 
-    const int gmax_all = std::max(1, (lmax_sel + 3) / 4);
-    const int erows_all = kBM + 4 * gmax_all + 8;
+    // the E4M3 form: one B term, 8 motif positions per k-step (K = 32); BF16: 4 (K = 16)
+    const bool e8 = terms == kE4M3;
+    const int kpos = e8 ? 8 : 4, nterm = e8 ? 1 : terms;
+    if (e8 && lmax_sel > kMaxE4M3Len)
+        return fail(ctx, BLAMM_ERR_UNSUPPORTED, "motif length %d exceeds the E4M3 form's limit %d", lmax_sel,
+                    kMaxE4M3Len);
+    const int gmax_all = std::max(1, (lmax_sel + kpos - 1) / kpos);
+    const int erows_all = kBM + kpos * gmax_all + 8;
     const long long smem_limit = (long long)ctx->max_smem;
     // everything but the B tiles (E stages, bias A tile, candidate staging, ...)
     const long long other = (long long)tc_smem_layout(0u, terms, erows_all, 256).total;
-    const long long b_term_cap = (smem_limit - other) / terms;
+    const long long b_term_cap = (smem_limit - other) / nterm;
     const int ncap = std::max(32, std::min(256, ctx->plan_nmax / 32 * 32));
     // widest tile whose B terms (g motif k-steps + 1 bias k-step) fit shared memory
     auto nmax_for = [&](int g) {
@@ -270,12 +340,12 @@ static int build_plan(blamm_ctx *ctx, int terms)
     // the best: 8 candidates per end column instead of 256, same optimum.
     for (int j = 1; j <= nsel; ++j) {
         const int L = ctx->len[order[j - 1]];
-        const int g = std::max(1, (L + 3) / 4);
-        const int bias = bias_folds(L) ? 0 : 1;
+        const int g = std::max(1, (L + kpos - 1) / kpos);
+        const int bias = !e8 && bias_folds(L) ? 0 : 1;
         for (int N = 32; N <= 256; N += 32) {
             if (N > nmax_for(g)) break;
             const int i = std::max(0, j - N);
-            const double mma = (terms * g + bias) * N / 2.0, epi = 1.0 * N;
+            const double mma = (nterm * g + bias) * N / 2.0, epi = 1.0 * N;
             const double cost = std::max(std::max(mma, epi), 300.0) + ctx->plan_job_cost;
             if (f[i] + cost < f[j]) {
                 f[j] = f[i] + cost;
@@ -298,23 +368,33 @@ static int build_plan(blamm_ctx *ctx, int terms)
         ctx->colq_guard.assign(ncols, 0.0);
         ctx->colq_off.assign(ncols + 1, 0);
         for (int c = 0; c < ncols; ++c) ctx->colq_off[c + 1] = ctx->colq_off[c] + 4 * (uint32_t)ctx->len[c];
-        ctx->colq_hi.assign(ctx->colq_off[ncols], 0);
+        ctx->colq_hi.assign(e8 ? 0 : ctx->colq_off[ncols], 0);
         ctx->colq_lo.assign(terms == 2 ? ctx->colq_off[ncols] : 0, 0);
+        ctx->colq_e8.assign(e8 ? ctx->colq_off[ncols] : 0, 0);
         for (int c = 0; c < ncols; ++c) {
             const float *col = &ctx->P[(size_t)c * ctx->p_rows];
             const int L = ctx->len[c];
-            const int k = 7 - column_exponent(col, L);
+            // BF16: grid 2^-k with |P| <= 128 * 2^-k; E4M3: scale 2^k with max|P| 2^k in (32, 64]
+            const int k = (e8 ? 6 : 7) - column_exponent(col, L);
             ctx->colq_k[c] = k;
             double eq = 0.0, a = 0.0;
             for (int j = 0; j < L; ++j) {
                 double mres = 0.0, mabs = 0.0;
                 for (int b = 0; b < 4; ++b) {
                     const double v = col[4 * j + b];
-                    const double hi = q_hi(v, k);
-                    const double lo = terms == 2 ? q_lo(v - hi, k) : 0.0;
-                    ctx->colq_hi[ctx->colq_off[c] + 4 * j + b] = bf16_bits_exact(hi);
-                    if (terms == 2) ctx->colq_lo[ctx->colq_off[c] + 4 * j + b] = bf16_bits_exact(lo);
-                    mres = std::max(mres, std::fabs(v - hi - lo));
+                    double q;
+                    if (e8) {
+                        const uint8_t code = e4m3_round(std::ldexp(v, k));
+                        ctx->colq_e8[ctx->colq_off[c] + 4 * j + b] = code;
+                        q = std::ldexp((double)e4m3_units(code), -9 - k);
+                    } else {
+                        const double hi = q_hi(v, k);
+                        const double lo = terms == 2 ? q_lo(v - hi, k) : 0.0;
+                        ctx->colq_hi[ctx->colq_off[c] + 4 * j + b] = bf16_bits_exact(hi);
+                        if (terms == 2) ctx->colq_lo[ctx->colq_off[c] + 4 * j + b] = bf16_bits_exact(lo);
+                        q = hi + lo;
+                    }
+                    mres = std::max(mres, std::fabs(v - q));
                     mabs = std::max(mabs, std::fabs(v));
                 }
                 eq += mres;
@@ -339,7 +419,10 @@ static int build_plan(blamm_ctx *ctx, int terms)
     // ((i/8 * 2(g+1) + kk/8) * 8 + i%8) * 8 + kk%8.  The hi term holds the bias,
     // -T split into three BF16-exact pieces on the column's grid, in K indices
     // 16g..16g+2 (the bias MMA's k-step) or, in a folded tile, 16g-8..16g-6 (the
-    // second K core of k-step g-1, which no motif of the tile reaches).
+    // second K core of k-step g-1, which no motif of the tile reaches).  The E4M3 form
+    // (1 byte per element, 16 per core row): byte ((i/8 * 2(g+1) + kk/16) * 8 + i%8) * 16
+    // + kk%16, K index 4j + b for position j, base b; the bias k-step (K 32g..32g+31)
+    // holds -T x 2^k (T on the grid 2^-(9+k)) as up to 32 E4M3 pieces.
     std::vector<TileDesc> tiles;
     std::vector<int32_t> slot_col;
     std::vector<uint8_t> bbuf;
@@ -350,18 +433,51 @@ static int build_plan(blamm_ctx *ctx, int terms)
     for (auto &sp : spans) {
         const int cnt = sp.second - sp.first;
         const int L = ctx->len[order[sp.second - 1]];
-        const int g = std::max(1, (L + 3) / 4);
+        const int g = std::max(1, (L + kpos - 1) / kpos);
         const int N = (cnt + 31) / 32 * 32;
         TileDesc td{};
         td.slot0 = (int32_t)slot_col.size();
         td.n = N;
         td.g = g;
-        td.b_bytes = N * 16 * (g + 1) * 2;
-        td.fold = bias_folds(L) ? 1 : 0;
+        td.b_bytes = N * 32 * (g + 1);  // 32 bytes per column and k-step in both forms
+        td.fold = !e8 && bias_folds(L) ? 1 : 0;
         const int kb = td.fold ? 16 * g - 8 : 16 * g;  // K index of the first bias piece
         size_t off = (bbuf.size() + 1023) / 1024 * 1024;
         td.b_off = (int64_t)off;
-        bbuf.resize(off + (size_t)td.b_bytes * terms, 0);
+        bbuf.resize(off + (size_t)td.b_bytes * nterm, 0);
+        if (e8) {
+            uint8_t *b8 = bbuf.data() + off;
+            auto at = [&](int i, int kk) {
+                return ((size_t)((i / 8) * 2 * (g + 1) + kk / 16) * 8 + i % 8) * 16 + kk % 16;
+            };
+            for (int i = 0; i < N; ++i) {
+                const int c = i < cnt ? order[sp.first + i] : -1;
+                slot_col.push_back(c);
+                // T x 2^k in units of 2^-9, kept within the scores a window can reach
+                // (|sum q| x 2^k <= 64 L): below it every window is a candidate, above it none
+                // is (a padding column: T = 1.0, never a candidate)
+                int64_t Tint = 512;
+                if (c >= 0) {
+                    const int k = kcol[c];
+                    const double lim = (double)(64 * ctx->len[c] + 1) * 512.0;
+                    const double t = ((double)ctx->thr[c] - guard_d[c]) * std::ldexp(1.0, 9 + k);
+                    Tint = std::isnan(t) ? (int64_t)lim : (int64_t)std::floor(std::max(-lim, std::min(lim, t)));
+                    ctx->bias_T[c] = std::ldexp((double)Tint, -9 - k);
+                }
+                uint8_t pcs[32];
+                const int np = e4m3_pieces(-Tint, pcs, 32);
+                if (np < 0) return fail(ctx, BLAMM_ERR_UNSUPPORTED, "E4M3 bias of column %d needs over 32 pieces", c);
+                for (int q = 0; q < np; ++q) b8[at(i, 32 * g + q)] = pcs[q];
+                if (c < 0) continue;
+                const uint32_t o = ctx->colq_off[c], nk = ctx->colq_off[c + 1] - o;
+                for (uint32_t kk = 0; kk < nk; ++kk) b8[at(i, (int)kk)] = ctx->colq_e8[o + kk];
+            }
+            tiles.push_back(td);
+            gmax = std::max(gmax, g);
+            btmax = std::max<uint32_t>(btmax, (uint32_t)td.b_bytes);
+            nmax = std::max(nmax, N);
+            continue;
+        }
         uint16_t *b_hi = reinterpret_cast<uint16_t *>(bbuf.data() + off);
         uint16_t *b_lo = terms == 2 ? reinterpret_cast<uint16_t *>(bbuf.data() + off + td.b_bytes) : nullptr;
         auto elem = [&](int i, int kk) {
@@ -413,7 +529,7 @@ static int build_plan(blamm_ctx *ctx, int terms)
                        cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
     ctx->tiles = tiles;
-    ctx->erows = kBM + 4 * gmax + 8;
+    ctx->erows = kBM + kpos * gmax + 8;
     ctx->b_term_max = btmax;
     ctx->tmem_cols = 512u;  // the whole TMEM: 4 accumulators of <= 128 columns or 2 of <= 256
     ctx->acc_stages = nmax <= 128 ? 4 : 2;
@@ -460,7 +576,10 @@ int blamm_ctx_create(int device, blamm_ctx **out)
                               (const void *)scan_tc_kernel<true, false, 1>,
                               (const void *)scan_tc_kernel<true, false, 2>,
                               (const void *)scan_tc_kernel<false, true, 1>,
-                              (const void *)scan_tc_kernel<false, true, 2>}) {
+                              (const void *)scan_tc_kernel<false, true, 2>,
+                              (const void *)scan_tc_kernel<false, false, kE4M3>,
+                              (const void *)scan_tc_kernel<true, false, kE4M3>,
+                              (const void *)scan_tc_kernel<false, true, kE4M3>}) {
             CK(cudaFuncGetAttributes(&fa, k));
             if (fa.maxThreadsPerBlock < kTcThreads)
                 return fail(ctx, BLAMM_ERR_UNSUPPORTED,
@@ -576,7 +695,8 @@ const char *blamm_last_error(const blamm_ctx *ctx) { return ctx ? ctx->err.c_str
 int blamm_set_mode(blamm_ctx *ctx, int mode)
 {
     if (!ctx) return BLAMM_ERR_ARG;
-    if (mode != BLAMM_MODE_FP32 && mode != BLAMM_MODE_BF16 && mode != BLAMM_MODE_BF16X2 && mode != BLAMM_MODE_AUTO)
+    if (mode != BLAMM_MODE_FP32 && mode != BLAMM_MODE_BF16 && mode != BLAMM_MODE_BF16X2 && mode != BLAMM_MODE_AUTO &&
+        mode != BLAMM_MODE_E4M3)
         return fail(ctx, BLAMM_ERR_ARG, "unknown mode %d", mode);
     ctx->mode = mode;
     return BLAMM_OK;
@@ -671,7 +791,10 @@ int blamm_set_thresholds(blamm_ctx *ctx, const float *thr)
 // BF16 terms of the tensor-core modes
 static int mode_terms(const blamm_ctx *ctx)
 {
-    return ctx->mode == BLAMM_MODE_BF16X2 ? 2 : ctx->mode == BLAMM_MODE_AUTO ? ctx->auto_terms : 1;
+    return ctx->mode == BLAMM_MODE_BF16X2 ? 2
+           : ctx->mode == BLAMM_MODE_E4M3  ? kE4M3
+           : ctx->mode == BLAMM_MODE_AUTO  ? ctx->auto_terms
+                                           : 1;
 }
 
 static int ensure_plan(blamm_ctx *ctx)
@@ -681,10 +804,11 @@ static int ensure_plan(blamm_ctx *ctx)
     return build_plan(ctx, terms);
 }
 
-// The tensor-core scan runs over windows of at most kEWindow positions: per window the
-// one-hot entries of its positions (e16_kernel, 16 B each) and one scan launch, so the entry
-// array holds one window (64 MB) whatever the stream length.  A window's scan reads up to
-// entry (its positions) + 127 + 4 * 64 + 2, and e16_kernel reads base i + 1 of the padded
+// The tensor-core scan runs over windows of at most ctx->ewindow positions (16 Mi by
+// default): per window the one-hot entries of its positions (e16_kernel or e8_kernel, 16 B
+// each) and one scan launch, so the entry array holds one window (256 MB) whatever the stream
+// length.  A window's scan reads up to entry (its positions) + 127 + 4 * 64 + 2 (BF16) or
+// + 127 + 8 * 32 + 3 (E4M3), and the entry kernels read up to base i + 3 of the padded
 // stream: entries = positions + kStreamPad - 64 stay inside both.
 static int64_t e16_entries(const blamm_ctx *ctx, int64_t n) { return std::min(n, ctx->ewindow) + kStreamPad - 64; }
 
@@ -785,6 +909,7 @@ template <bool kDump, bool kProf>
 static void launch_tc_as(const TcParams &p, int grid, uint32_t smem, cudaStream_t st)
 {
     if (p.terms == 2) scan_tc_kernel<kDump, kProf, 2><<<grid, kTcThreads, smem, st>>>(p);
+    else if (p.terms == kE4M3) scan_tc_kernel<kDump, kProf, kE4M3><<<grid, kTcThreads, smem, st>>>(p);
     else scan_tc_kernel<kDump, kProf, 1><<<grid, kTcThreads, smem, st>>>(p);
 }
 
@@ -806,7 +931,8 @@ static int launch_tc_windows(blamm_ctx *ctx, TcParams p, const uint32_t *seq2, c
     for (int64_t m0 = 0; m0 < n_mtiles; m0 += wt) {
         const int64_t mt = std::min(wt, n_mtiles - m0), base = m0 * kBM;
         const int64_t ne = std::min(mt * kBM, n - base) + kStreamPad - 64;
-        e16_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, ctx->stream>>>(seq2, zmask, base, ne, e16);
+        if (p.terms == kE4M3) e8_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, ctx->stream>>>(seq2, zmask, base, ne, e16);
+        else e16_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, ctx->stream>>>(seq2, zmask, base, ne, e16);
         CK(cudaGetLastError());
         p.e16 = e16;
         p.n_mtiles = mt;
@@ -1596,7 +1722,9 @@ int blamm_debug_scores(blamm_ctx *ctx, const char *bases, int64_t n, int64_t p0,
         for (int64_t i = 0; rc == BLAMM_OK && i < npos; ++i)
             for (int c = 0; c < ctx->ncols; ++c) {
                 float &v = out[i * ctx->ncols + c];
-                v = (float)((double)v + ctx->bias_T[c]);
+                // the E4M3 form's accumulator is scaled by 2^k (exact: a power of two)
+                const double sv = ctx->plan_terms == kE4M3 ? std::ldexp((double)v, -ctx->colq_k[c]) : (double)v;
+                v = (float)(sv + ctx->bias_T[c]);
             }
     }
     cudaFree(d_dump);
@@ -1927,17 +2055,24 @@ int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t
     const double cost_opts[] = {200.0, 700.0, 1500.0};
     const int keep_nmax = ctx->plan_nmax, keep_terms = ctx->auto_terms;
     const double keep_cost = ctx->plan_job_cost;
-    // BLAMM_MODE_AUTO also chooses the number of BF16 terms: one term halves the MMAs
-    // and widens the guard band (more candidates to rescore), so the whole call's
-    // kernel time (packing, scan, rescoring) decides
-    const int nterm_opts = ctx->mode == BLAMM_MODE_AUTO ? 2 : 1;
+    // BLAMM_MODE_AUTO also chooses the form: one BF16 term halves the MMAs of two and
+    // widens the guard band (more candidates to rescore), one E4M3 term (motifs up to 64
+    // positions) halves them again with a still wider band, so the whole call's kernel
+    // time (packing, scan, rescoring) decides
+    int lmax_sel = 1;
+    if (ctx->active.empty())
+        for (int c = 0; c < ctx->ncols; ++c) lmax_sel = std::max(lmax_sel, ctx->len[c]);
+    else
+        for (const int c : ctx->active) lmax_sel = std::max(lmax_sel, ctx->len[c]);
+    int term_opts[3] = {1, 2, kE4M3};
+    const int nterm_opts = ctx->mode == BLAMM_MODE_AUTO ? (lmax_sel <= kMaxE4M3Len ? 3 : 2) : 1;
     float best = std::numeric_limits<float>::infinity();
     int bn = keep_nmax, bt = keep_terms;
     double bc = keep_cost;
     for (int ti = 0; ti < nterm_opts; ++ti)
         for (int nm : nmax_opts)
             for (double jc : cost_opts) {
-                if (ctx->mode == BLAMM_MODE_AUTO) ctx->auto_terms = ti + 1;
+                if (ctx->mode == BLAMM_MODE_AUTO) ctx->auto_terms = term_opts[ti];
                 ctx->plan_nmax = nm;
                 ctx->plan_job_cost = jc;
                 ctx->plan_valid = false;

@@ -51,7 +51,7 @@ void scanUsage()
                  "(default = 0.95)\n"
                  "  -pt\t--pthreshold\tcompute the motif score threshold from p-value [0..1] (default = 1E-4)\n"
                  "  -t\t--numthreads\tset the number of parallel threads [default = #cores]\n"
-                 "  -m\t--mode\t\tGPU arithmetic: auto (default), bf16x2, bf16 or fp32\n\n"
+                 "  -m\t--mode\t\tGPU arithmetic: auto (default), bf16x2, bf16, e4m3 or fp32\n\n"
                  " [file_options]\n"
                  "  -H\t--histdir\tdirectory where the histogram file(s) are stored [default = .]\n"
                  "  -o\t--output\tfilename for the motif occurrences [default = occurences.txt]\n\n"
@@ -440,7 +440,8 @@ int runScanModule(int argc, char **argv)
             else if (m == "bf16") o.mode = BLAMM_MODE_BF16;
             else if (m == "bf16x2") o.mode = BLAMM_MODE_BF16X2;
             else if (m == "auto") o.mode = BLAMM_MODE_AUTO;
-            else throw std::runtime_error("unknown mode " + m + " (auto, bf16x2, bf16 or fp32)");
+            else if (m == "e4m3") o.mode = BLAMM_MODE_E4M3;
+            else throw std::runtime_error("unknown mode " + m + " (auto, bf16x2, bf16, e4m3 or fp32)");
         } else {
             scanUsage();
             exit(EXIT_FAILURE);

@@ -217,6 +217,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
+// Instruction descriptor for kind::f8f6f4 with E4M3 A and B (format 0 in bits 7-9 and
+// 10-12), FP32 accumulate, both operands K-major, dense.
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(uint32_t M, uint32_t N)
+{
+    return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, one MMA of M x N x 16, issued by the one lane that
 // elect.sync picks in a converged warp: the warp runs the issuing loop together, so the
 // descriptors are warp-uniform values.  (The same loop run by one lane alone issued
@@ -229,6 +236,19 @@ __device__ __forceinline__ void mma_bf16_elect(uint32_t tmem_d, uint64_t adesc, 
         "elect.sync _|e, 0xffffffff;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// The same with E4M3 operands (kind::f8f6f4): one MMA of M x N x 32.
+__device__ __forceinline__ void mma_e4m3_elect(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                               uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p, e;\n\t"
+        "elect.sync _|e, 0xffffffff;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }

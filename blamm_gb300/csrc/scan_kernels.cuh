@@ -105,6 +105,28 @@ __device__ __forceinline__ uint2 onehot_bf16(uint32_t code, uint32_t zero)
     return make_uint2((code & 2u) ? 0u : h, (code & 2u) ? h : 0u);
 }
 
+// E4M3 one-hot of one base: byte `code` of the 4 is 1.0 (0x38), zeros for a zero-masked base.
+__device__ __forceinline__ uint32_t onehot_e4m3(uint32_t code, uint32_t zero)
+{
+    return zero ? 0u : 0x38u << (8 * code);
+}
+
+// E4M3 entries of one window: e8[i] = one-hot of bases base + i .. base + i + 3 (4 bytes
+// each, in that order: K slots 4u + code), i < ne.
+__global__ void e8_kernel(const uint32_t *__restrict__ seq2, const uint32_t *__restrict__ zmask, int64_t base,
+                          int64_t ne, uint4 *__restrict__ e8)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ne) return;
+    uint32_t w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t i = base + t + u;
+        w[u] = onehot_e4m3((seq2[i >> 4] >> (2 * (i & 15))) & 3u, (zmask[i >> 5] >> (i & 31)) & 1u);
+    }
+    e8[t] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 // Entries of one window of the stream: e16[i] = entry of position base + i, i < ne.
 __global__ void e16_kernel(const uint32_t *__restrict__ seq2, const uint32_t *__restrict__ zmask, int64_t base,
                            int64_t ne, uint4 *__restrict__ e16)

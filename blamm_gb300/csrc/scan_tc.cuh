@@ -3,8 +3,8 @@
 //
 // Score of motif column c at position p:  sum_j P(4j + base(p+j), c).
 // After packing, e16_kernel writes one 16-byte entry per stream position of a
-// window of at most 4 Mi positions (the scan runs once per window, so the entry
-// array stays 64 MB whatever the stream length),
+// window of at most 16 Mi positions (the scan runs once per window, so the entry
+// array stays 256 MB whatever the stream length),
 // E[i] = onehot(base i) ++ onehot(base i+1) (2 bases x 4 channels x bf16).
 // For an M tile of 128 positions starting at m0, a bulk copy brings entries
 // m0 .. m0+128+4g+1 into shared memory; read with row stride 16 B, 8-row group
@@ -30,12 +30,21 @@
 // of sum(P), so every reference hit is a candidate; candidates are rescored
 // in exact FP32 (rescore_kernel).
 //
+// The E4M3 form (kTerms == kE4M3, kind::f8f6f4, K = 32 per MMA) scores 8 motif
+// positions per k-step: e8_kernel's entries hold 4 bases (4 x 4 E4M3 bytes), the
+// A cores of a k-step are 4 entries apart (LBO 64 B) and k-steps 8 entries (128 B)
+// apart; B holds P(c) x 2^s_c rounded to E4M3 (s_c puts max|P_c| in (32, 64]),
+// so every product and partial sum is a multiple of 2^-9 below 2^15 in
+// magnitude, exact in FP32 when the tensor cores add exactly -- which the lane
+// check in the tests shows for these operands.  The bias MMA's A rows are 32
+// ones and its B column the pieces of T x 2^s_c.
+//
 // Roles (640 threads, warp w on SM sub-partition w % 4): warps 0-15 drain TMEM
 // (lane quarter = warp % 4, column group = warp / 4) and test for candidates;
-// warps 16 and 17 (one lane each) issue the MMAs of the even and the odd jobs,
-// so that one issuer's waits, commits and loop overhead overlap the other's
-// MMAs (a thread issues about one 128x256x16 MMA per 128 cycles, and a job's
-// result reaches the drain warps some 600 cycles after its last MMA); their
+// warps 16 and 17 issue the MMAs of the even and the odd jobs (the whole warp
+// runs the loop, one elected lane issues), so that one issuer's waits, commits
+// and loop overhead overlap the other's MMAs (a job's result reaches the drain
+// warps several hundred cycles after its last MMA is accepted); their
 // waits spin instead of sleeping, since a sleeping issuer wakes late; warp 18
 // (one lane) loads B tiles and E windows with TMA bulk copies up to kEStages
 // jobs ahead; warp 16 also allocates TMEM.
@@ -75,6 +84,8 @@ constexpr int kLoadWarp = 18;    // TMA bulk copies of B tiles and E windows
 constexpr int kRecBlock = kRecBlockSlots;  // candidate record slots a drain warp reserves at a time
 constexpr int kTcThreads = 640;  // 20 warps (registers are allocated per 4 warps)
 constexpr int kEStages = 6;      // E windows in flight
+constexpr int kE4M3 = 8;         // kTerms of the E4M3 form (one term, K = 32 per MMA)
+constexpr int kMaxE4M3Len = 64;  // longest motif of the E4M3 form (its bias needs <= 32 pieces)
 constexpr int kMaxAcc = 4;       // TMEM accumulator stages (at most)
 
 // Per-N-tile description (host-built, staged in SMEM by the kernel).
@@ -220,7 +231,8 @@ __device__ __forceinline__ long long tick()
 }
 
 // kDump: also write the raw accumulator of some positions (test hook);
-// kProf: role timing into p.prof; kTerms: p.terms (1 or 2).  The scan itself
+// kProf: role timing into p.prof; kTerms: p.terms (1 or 2 BF16 terms, or kE4M3,
+// one E4M3 term; B terms loaded: 2 for kTerms == 2, else 1).  The scan itself
 // is <false, false, p.terms>.  The issuing threads run once per MMA and per
 // job, so every branch taken out of their loops at compile time shows in the
 // scan time (runtime mode switches cost 2-4 %).
@@ -250,7 +262,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         // MMA reads [ones | zeros] (start = block, LBO = 2048 B)
         uint4 *ab = reinterpret_cast<uint4 *>(smem + L.abias);
         for (int i = threadIdx.x; i < 256; i += blockDim.x)
-            ab[i] = i < 128 ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+            ab[i] = kTerms == kE4M3 ? make_uint4(0x38383838u, 0x38383838u, 0x38383838u, 0x38383838u)
+                    : i < 128      ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u)
+                                   : make_uint4(0u, 0u, 0u, 0u);
     }
     if (threadIdx.x == 0) {
         for (int s = 0; s < kEStages; ++s) {
@@ -294,7 +308,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
         long long t_acc = 0, t_w = 0, t_b = 0;
         const long long t_start = tick<kProf>();
         const uint64_t adesc_bias = ptx::smem_desc(sbase + L.abias, 2048u, 128u);
-        const uint64_t adesc_e = ptx::smem_desc(sbase + L.e0, 32u, 128u);
+        // A of a k-step: its two K cores 2 (BF16) or 4 (E4M3) entries apart; k-steps 4 or 8
+        // entries apart (a_step, in 16 B units)
+        const uint64_t adesc_e = ptx::smem_desc(sbase + L.e0, kTerms == kE4M3 ? 64u : 32u, 128u);
+        const uint32_t a_step = kTerms == kE4M3 ? 8u : 4u;
+        auto mma = [&](uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+            if constexpr (kTerms == kE4M3) ptx::mma_e4m3_elect(d, a, b, idesc, acc);
+            else ptx::mma_bf16_elect(d, a, b, idesc, acc);
+        };
         const uint32_t e_step = (uint32_t)p.erows;  // one E stage in 16 B units
         uint32_t jc = 0;
         bool ok = true;
@@ -316,7 +337,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 const TileDesc td = s_tiles[tile];
                 g_steps = (uint32_t)td.g;
                 fold = (uint32_t)td.fold;
-                idesc = ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
+                idesc = kTerms == kE4M3 ? ptx::idesc_e4m3_f32(kBM, (uint32_t)td.n)
+                                        : ptx::idesc_bf16_f32(kBM, (uint32_t)td.n);
                 const uint32_t sbo_b = 256u * (g_steps + 1);  // bytes between 8-column groups of B
                 bdesc_hi0 = ptx::smem_desc(sbase + L.b_hi, 128u, sbo_b);
                 bdesc_lo0 = ptx::smem_desc(sbase + L.b_lo, 128u, sbo_b);
@@ -345,20 +367,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     acc = g_plain > 0u ? 1u : 0u;
                 } else {
                     // D = -T (bias pieces in the extra k-step g of the hi term)
-                    ptx::mma_bf16_elect(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, idesc, 0u);
+                    mma(d_tmem, adesc_bias, bdesc_hi0 + 16u * g_steps, 0u);
                 }
                 for (uint32_t g = 0; g < g_plain; ++g) {
                     const uint32_t a = (g == 0u && fold) ? 0u : 1u;  // a folded tile starts at D = A B
-                    ptx::mma_bf16_elect(d_tmem, adesc0 + 4u * g, bdesc_hi0 + 16u * g, idesc, a);
-                    if (kTerms == 2) ptx::mma_bf16_elect(d_tmem, adesc0 + 4u * g, bdesc_lo0 + 16u * g, idesc, 1u);
+                    mma(d_tmem, adesc0 + a_step * g, bdesc_hi0 + 16u * g, a);
+                    if (kTerms == 2) mma(d_tmem, adesc0 + a_step * g, bdesc_lo0 + 16u * g, 1u);
                 }
                 if (fold) {
                     // k-step g-1: first K core = entries m0 + 4(g-1) + r, second K core = the
                     // constant rows (the hi term's B holds the bias pieces there)
-                    const uint32_t a_last = sbase + L.e0 + es * e_step * 16u + 64u * g_plain;
+                    const uint32_t a_last = sbase + L.e0 + es * e_step * 16u + 16u * a_step * g_plain;
                     const uint64_t adesc_last = ptx::smem_desc(a_last, sbase + L.abias - a_last, 128u);
-                    ptx::mma_bf16_elect(d_tmem, adesc_last, bdesc_hi0 + 16u * g_plain, idesc, acc);
-                    if (kTerms == 2) ptx::mma_bf16_elect(d_tmem, adesc_last, bdesc_lo0 + 16u * g_plain, idesc, 1u);
+                    mma(d_tmem, adesc_last, bdesc_hi0 + 16u * g_plain, acc);
+                    if (kTerms == 2) mma(d_tmem, adesc_last, bdesc_lo0 + 16u * g_plain, 1u);
                 }
                 ptx::mma_commit_elect(bars + 8 * (BAR_WEMPTY + es));
                 ptx::mma_commit_elect(bars + 8 * (BAR_AFULL + s));
@@ -402,7 +424,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                     if (!ok) break;
                     // the previous B copy has landed (both issuers waited for it)
                 }
-                ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * kTerms);
+                ptx::mbar_arrive_expect_tx(bars + 8 * BAR_BFULL, (uint32_t)td.b_bytes * (kTerms == 2 ? 2u : 1u));
                 ptx::bulk_g2s(sbase + L.b_hi, p.bbuf + td.b_off, (uint32_t)td.b_bytes, bars + 8 * BAR_BFULL);
                 if (kTerms == 2)
                     ptx::bulk_g2s(sbase + L.b_lo, p.bbuf + td.b_off + td.b_bytes, (uint32_t)td.b_bytes,
@@ -411,12 +433,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) scan_tc_kernel(TcParams p)
                 bphase ^= 1;
                 cur_tile = tile;
             }
-            // E window of this job: entries m0 .. m0 + 128 + 4g + 1 (16 B each)
+            // E window of this job (16 B entries)
             const long long t0 = tick<kProf>();
             ok = ptx::mbar_wait(bars + 8 * (BAR_WEMPTY + es), eph ^ 1u, s_abort, p.wait_limit);
             if (kProf) t_we += tick<kProf>() - t0;
             if (!ok) break;
-            const uint32_t bytes = 16u * (uint32_t)(kBM + 4 * td.g + 2);
+            // entries m0 .. m0 + 128 + 4g + 1 (BF16) or m0 + 128 + 8g + 3 (E4M3)
+            const uint32_t bytes = 16u * (uint32_t)(kTerms == kE4M3 ? kBM + 8 * td.g + 4 : kBM + 4 * td.g + 2);
             ptx::mbar_arrive_expect_tx(bars + 8 * (BAR_WFULL + es), bytes);
             ptx::bulk_g2s(sbase + L.e0 + es * (uint32_t)p.erows * 16u, p.e16 + (int64_t)it.m * kBM, bytes,
                           bars + 8 * (BAR_WFULL + es));

@@ -46,8 +46,12 @@ extern "C" {
 #define BLAMM_MODE_FP32 0   /* plain SIMT FP32 sums: the straightforward GPU form */
 #define BLAMM_MODE_BF16 1   /* tcgen05, P as one BF16 term, wide guard band */
 #define BLAMM_MODE_BF16X2 2 /* tcgen05, P split hi+lo BF16 (two MMAs), narrow guard band */
-#define BLAMM_MODE_AUTO 3   /* tcgen05 with one or two BF16 terms, whichever blamm_autotune
-                               measured faster on its sample (one term until then) */
+#define BLAMM_MODE_AUTO 3   /* tcgen05 with one or two BF16 terms or E4M3, whichever
+                               blamm_autotune measured faster on its sample (one BF16 term
+                               until then) */
+#define BLAMM_MODE_E4M3 4   /* tcgen05 kind::f8f6f4: P x 2^k (max |P| 2^k in (32, 64]) as one
+                               E4M3 term, 8 motif positions per MMA, widest guard band;
+                               motifs up to 64 positions */
 
 typedef struct blamm_ctx blamm_ctx;
 
@@ -175,7 +179,8 @@ void blamm_scan_graph_destroy(void *graph);
 /* Autotuner: time the tensor-core scan of the first min(n, 16 Mi) positions
  * (device data) under several tile plans -- widest N tile 128 / 192 / 256 x
  * the planner's fixed cost per job, and in BLAMM_MODE_AUTO one and two BF16
- * terms -- and keep the fastest for later scans of this context (the time of
+ * terms and one E4M3 term (motifs up to 64 positions) -- and keep the fastest
+ * for later scans of this context (the time of
  * all kernels of the call: packing, scan, rescoring; median of three).
  * *best_ms (optional) receives that time.  Nothing to tune in BLAMM_MODE_FP32.
  * The chosen term count: blamm_get_terms. */
@@ -186,7 +191,8 @@ int blamm_autotune(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t
  * columns; at most 128 gives four TMEM accumulators instead of two) and the
  * fixed cycles per job of its cost model.  Setting them replans. */
 int blamm_set_plan_options(blamm_ctx *ctx, int max_tile_columns, float job_cost);
-/* BF16 terms the tensor-core scan uses in the current mode (1 or 2; 0 for FP32). */
+/* The tensor-core form of the current mode: 1 or 2 BF16 terms, 8 for one E4M3 term
+ * (BLAMM_MODE_E4M3, or BLAMM_MODE_AUTO after the autotuner chose it); 0 for FP32. */
 int blamm_get_terms(const blamm_ctx *ctx);
 int blamm_get_plan_options(const blamm_ctx *ctx, int *max_tile_columns, float *job_cost);
 

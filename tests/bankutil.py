@@ -49,8 +49,18 @@ def make_stream(seed: int, n: int, nruns: int = 1, lower_frac: float = 0.0,
     return b, runs
 
 
+def e4m3_round(x: np.ndarray) -> np.ndarray:
+    """Nearest E4M3 value (3 mantissa bits, ties to even; subnormals on the grid 2^-9;
+    |x| <= 448 assumed)."""
+    a = np.abs(x)
+    e = np.floor(np.log2(np.where(a > 0, a, 1.0)))
+    ulp = np.where(a < 2.0 ** -6, 2.0 ** -9, 2.0 ** (e - 3))
+    return np.sign(x) * np.round(a / ulp) * ulp
+
+
 def quantized_columns(P: np.ndarray, lens: np.ndarray, terms: int) -> np.ndarray:
-    """The fixed-point BF16 terms the tensor cores see (hi [+ lo]), as float64."""
+    """The terms the tensor cores see, as float64: fixed-point BF16 hi [+ lo] (terms 1, 2),
+    or (terms 8) P x 2^k rounded to E4M3 with max |P| 2^k in (32, 64], divided by 2^k."""
     out = np.zeros(P.shape, dtype=np.float64)
     for c in range(P.shape[0]):
         v = P[c, :4 * lens[c]].astype(np.float64)
@@ -61,6 +71,10 @@ def quantized_columns(P: np.ndarray, lens: np.ndarray, terms: int) -> np.ndarray
             e = max(-30, min(40, e))
         else:
             e = -30
+        if terms == 8:
+            k = 6 - e
+            out[c, :4 * lens[c]] = e4m3_round(np.ldexp(v, k)) * 2.0 ** -k
+            continue
         k = 7 - e
         hi = np.rint(np.ldexp(v, k)) * 2.0 ** -k
         q = hi

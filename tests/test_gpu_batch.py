@@ -12,7 +12,7 @@ from blamm_gb300 import HIT_DTYPE
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["bf16x2", "bf16", "fp32"]
+MODES = ["bf16x2", "bf16", "e4m3", "fp32"]
 
 
 def _torch():

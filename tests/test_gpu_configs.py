@@ -43,7 +43,7 @@ def markov_case():
     return _markov_case(31, 1_200_000, 120)
 
 
-@pytest.mark.parametrize("mode", ["auto", "bf16", "bf16x2"])
+@pytest.mark.parametrize("mode", ["auto", "bf16", "bf16x2", "e4m3"])
 @pytest.mark.parametrize("pi", [0, 1])
 def test_markov_n_runs_stream_matches_oracle(markov_case, mode, pi):
     bases, runs, P, lens, thr = markov_case

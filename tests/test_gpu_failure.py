@@ -15,7 +15,7 @@ from blamm_gb300._native import BLAMM_ERR_TIMEOUT
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16", "e4m3"])
 def test_a_wait_that_runs_out_reports_timeout_and_the_context_stays_usable(scanner, mode):
     P, lens, thr = make_bank(81, 48, 5, 30, rel=0.85)
     bases, runs = make_stream(82, 400_000, nruns=5)

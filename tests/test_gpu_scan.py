@@ -11,10 +11,11 @@ from bankutil import exact_window_scores, make_bank, make_stream, quantized_colu
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["bf16x2", "bf16", "fp32"]
+MODES = ["bf16x2", "bf16", "e4m3", "fp32"]
+TERMS = {"bf16x2": 2, "bf16": 1, "e4m3": 8}
 
 
-@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16", "e4m3"])
 def test_tensor_core_sums_are_exact(scanner, mode):
     """The raw accumulator equals the exact sum of the fixed-point BF16 terms (no rounding)."""
     P, lens, thr = make_bank(1, 40, 5, 30)
@@ -23,14 +24,14 @@ def test_tensor_core_sums_are_exact(scanner, mode):
     scanner.set_motifs(P, lens, thr)
     p0, npos = 100, 700
     D = scanner.debug_scores(bases, p0, npos)
-    Q = quantized_columns(P, lens, 2 if mode == "bf16x2" else 1)
+    Q = quantized_columns(P, lens, TERMS[mode])
     want = exact_window_scores(bases, Q, lens, p0, npos)
     assert np.all(np.float64(np.float32(want)) == want)  # representable
     bad = np.flatnonzero(D.astype(np.float64).ravel() != want.ravel())
     assert bad.size == 0, f"{bad.size} mismatches, first {D.ravel()[bad[0]]} vs {want.ravel()[bad[0]]}"
 
 
-@pytest.mark.parametrize("mode", ["bf16x2", "bf16"])
+@pytest.mark.parametrize("mode", ["bf16x2", "bf16", "e4m3"])
 @pytest.mark.parametrize("lengths", [(1, 2), (3, 4), (5, 6), (7, 8), (1, 10), (13, 14), (29, 30)])
 def test_bias_in_the_last_k_step(scanner, mode, lengths):
     """A tile whose longest motif has length 4g-3 or 4g-2 carries the threshold bias in the
@@ -44,7 +45,7 @@ def test_bias_in_the_last_k_step(scanner, mode, lengths):
     scanner.set_motifs(P, lens, thr)
     p0, npos = 40, 600
     D = scanner.debug_scores(bases, p0, npos)
-    Q = quantized_columns(P, lens, 2 if mode == "bf16x2" else 1)
+    Q = quantized_columns(P, lens, TERMS[mode])
     want = exact_window_scores(bases, Q, lens, p0, npos)
     bad = np.flatnonzero(D.astype(np.float64).ravel() != want.ravel())
     assert bad.size == 0, f"{bad.size} mismatches, first {D.ravel()[bad[0]]} vs {want.ravel()[bad[0]]}"
@@ -83,6 +84,11 @@ def test_long_motifs_and_single_column(scanner, mode):
     bases, runs = make_stream(8, 20_000, nruns=3)
     scanner.set_mode(mode)
     scanner.set_motifs(P, lens, thr)
+    if mode == "e4m3":  # the E4M3 form takes motifs up to 64 positions
+        from blamm_gb300 import BlammError
+        with pytest.raises(BlammError):
+            scanner.scan(bases, runs)
+        return
     ok, msg = same_hits(scanner.scan(bases, runs), oracle.scan(bases, runs, P, lens, thr))
     assert ok, msg
     P1, l1, t1 = P[:1], lens[:1], thr[:1]
