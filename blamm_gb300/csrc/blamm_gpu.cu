@@ -394,13 +394,15 @@ static int build_plan(blamm_ctx *ctx, int terms)
                         if (terms == 2) ctx->colq_lo[ctx->colq_off[c] + 4 * j + b] = bf16_bits_exact(lo);
                         q = hi + lo;
                     }
-                    mres = std::max(mres, std::fabs(v - q));
+                    // only P > q can put a reference hit below T: sum(q) = sum(P) - sum(P - q)
+                    mres = std::max(mres, v - q);
                     mabs = std::max(mabs, std::fabs(v));
                 }
                 eq += mres;
                 a += mabs;
             }
-            // |fl(sequential sum) - exact sum| <= gamma_{L-1} * sum|terms|
+            // guard = sum_j max_b (P - q)^+ (mres starts at 0) + the bound on the reference's
+            // own rounding, |fl(sequential sum) - exact sum| <= gamma_{L-1} * sum|terms|
             const double u = std::ldexp(1.0, -24);
             const double nl = std::max(0, L - 1);
             const double gamma = nl * u / (1.0 - nl * u);
