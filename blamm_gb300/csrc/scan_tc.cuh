@@ -33,10 +33,10 @@
 // The E4M3 form (kTerms == kE4M3, kind::f8f6f4, K = 32 per MMA) scores 8 motif
 // positions per k-step: e8_kernel's entries hold 4 bases (4 x 4 E4M3 bytes), the
 // A cores of a k-step are 4 entries apart (LBO 64 B) and k-steps 8 entries (128 B)
-// apart; B holds P(c) x 2^s_c rounded to E4M3 (s_c puts max|P_c| in (32, 64]),
-// so every product and partial sum is a multiple of 2^-9 below 2^15 in
-// magnitude, exact in FP32 when the tensor cores add exactly -- which the lane
-// check in the tests shows for these operands.  The bias MMA's A rows are 32
+// apart; B holds P(c) x 2^s_c rounded to E4M3 (s_c puts max|P_c| 2^s_c in
+// (32, 64]), so every product and partial sum is a multiple of 2^-9 below 2^13
+// in magnitude (motifs up to 64 positions), exact in FP32 when the tensor cores
+// add exactly -- which the lane check in the tests shows for these operands.  The bias MMA's A rows are 32
 // ones and its B column the pieces of T x 2^s_c.
 //
 // Roles (640 threads, warp w on SM sub-partition w % 4): warps 0-15 drain TMEM
@@ -63,7 +63,8 @@
 // interleaved over the CTAs, N-tile major, so a CTA reloads B only when its
 // tile changes: both issuers commit their old-tile MMAs to a tile-done
 // barrier, the loader then copies the new B, and both wait for it.  Every wait
-// is an mbarrier try-wait that sleeps and is bounded: on a timeout the CTA
+// is bounded (the issuers poll with test_wait, the drain warps wait with try_wait
+// without a suspend hint, the loader's try_wait sleeps): on a timeout the CTA
 // raises an abort flag, every role stops, copies and MMAs in flight are
 // drained, TMEM is freed and the status word tells the host.
 #pragma once
