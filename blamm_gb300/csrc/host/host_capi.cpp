@@ -9,6 +9,7 @@
 #include "blamm_host.h"
 #include "format.h"
 #include "histogram.h"
+#include "ingest.h"
 #include "motif.h"
 #include "sequence.h"
 
@@ -231,5 +232,44 @@ const char *blamm_fasta_sequence_name(const blamm_fasta *f, int64_t i)
 }
 
 void blamm_fasta_close(blamm_fasta *f) { delete f; }
+
+struct blamm_fasta_pieces {
+    blamm::FastaPieceReader reader;
+    std::string piece;
+    blamm_fasta_pieces(std::vector<std::string> files, size_t bytes) : reader(std::move(files), bytes) {}
+};
+
+int blamm_fasta_pieces_open(const char *const *files, int nfiles, int64_t piece_bytes, blamm_fasta_pieces **out)
+{
+    if (!files || nfiles < 0 || piece_bytes <= 0 || !out) return -1;
+    return guarded([&] {
+        std::vector<std::string> v(files, files + nfiles);
+        *out = new blamm_fasta_pieces(v, (size_t)piece_bytes);
+    });
+}
+
+int blamm_fasta_pieces_next(blamm_fasta_pieces *p, const char **text, int64_t *size)
+{
+    if (!p || !text || !size) return -1;
+    int got = 0;
+    const int rc = guarded([&] { got = p->reader.next(p->piece) ? 1 : 0; });
+    if (rc < 0) return rc;
+    *text = got ? p->piece.data() : nullptr;
+    *size = got ? (int64_t)p->piece.size() : 0;
+    return got;
+}
+
+void blamm_fasta_pieces_close(blamm_fasta_pieces *p) { delete p; }
+
+int blamm_fasta_header_name(const char *text, int64_t size, int64_t header_pos, char *out, int cap)
+{
+    if (!text || size < 0 || header_pos < 0 || header_pos >= size || !out || cap <= 0) return -1;
+    const std::string t(text, (size_t)size);
+    const std::string name = blamm::headerNames(t, {header_pos})[0];
+    if ((int64_t)name.size() + 1 > cap) return -1;
+    std::memcpy(out, name.data(), name.size());
+    out[name.size()] = 0;
+    return (int)name.size();
+}
 
 }  // extern "C"

@@ -85,6 +85,21 @@ int64_t blamm_fasta_num_sequences(const blamm_fasta *f);
 const char *blamm_fasta_sequence_name(const blamm_fasta *f, int64_t i);
 void blamm_fasta_close(blamm_fasta *f);
 
+/* FASTA text in pieces for a device parser (the command line's GPU reader,
+ * blamm_stream_load_fasta): the files' text in order, a newline added to a file
+ * that lacks a final one, cut only where a header line starts, each piece at least
+ * piece_bytes long (the last may be shorter).  No sequence spans two pieces.
+ * _next returns 1 and the piece (valid until the next call), 0 at the end, <0 on
+ * error (a file that cannot be opened: blamm_host_last_error). */
+typedef struct blamm_fasta_pieces blamm_fasta_pieces;
+int blamm_fasta_pieces_open(const char *const *files, int nfiles, int64_t piece_bytes, blamm_fasta_pieces **out);
+int blamm_fasta_pieces_next(blamm_fasta_pieces *p, const char **text, int64_t *size);
+void blamm_fasta_pieces_close(blamm_fasta_pieces *p);
+/* The sequence name of the header line at byte offset header_pos of text (the first
+ * whitespace-delimited token after '>', as the reference reads it), zero-terminated
+ * into out (cap bytes); returns its length, or -1 if it does not fit. */
+int blamm_fasta_header_name(const char *text, int64_t size, int64_t header_pos, char *out, int cap);
+
 #ifdef __cplusplus
 }
 #endif

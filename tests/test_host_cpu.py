@@ -324,3 +324,71 @@ def test_oracle_bank_equals_product_bank():
     want = {(int(bank.name(c)[1:]), int(rcb[c])): (Pb[c, :4 * lb[c]].tobytes(), tb[0][c], tb[1][c])
             for c in range(len(lb))}
     assert got == want
+
+
+def _pieces(files, piece_bytes):
+    L = C.CDLL(os.path.join(ROOT, "blamm_gb300", "_build", "libblamm_host.so"))
+    L.blamm_fasta_pieces_open.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.c_int64, C.POINTER(C.c_void_p)]
+    L.blamm_fasta_pieces_next.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]
+    L.blamm_fasta_pieces_close.argtypes = [C.c_void_p]
+    h = C.c_void_p()
+    arr = (C.c_char_p * len(files))(*[f.encode() for f in files])
+    assert L.blamm_fasta_pieces_open(arr, len(files), piece_bytes, C.byref(h)) == 0
+    out = []
+    while True:
+        t, n = C.c_void_p(), C.c_int64()
+        rc = L.blamm_fasta_pieces_next(h, C.byref(t), C.byref(n))
+        assert rc >= 0
+        if rc == 0:
+            break
+        out.append(C.string_at(t, n.value))
+    L.blamm_fasta_pieces_close(h)
+    return out
+
+
+@pytest.mark.parametrize("piece_bytes", [1, 7, 100, 5000, 1 << 26])
+def test_fasta_pieces_cut_only_at_header_lines(tmp_path, piece_bytes):
+    """The GPU reader's pieces: the files' text in order (a final newline added where a file
+    lacks one), each piece but the last at least piece_bytes long and ending right before a
+    header line, with no header line starting past piece_bytes inside it."""
+    rng = np.random.default_rng(piece_bytes)
+    files, want = [], b""
+    for fi in range(5):
+        parts = []
+        if fi == 3:  # a file that continues the previous file's last sequence
+            parts.append(b"ACGTNNacgt\n")
+        for si in range(int(rng.integers(0, 4))):
+            parts.append(f">f{fi}s{si} descr\n".encode())
+            for _ in range(int(rng.integers(0, 5))):
+                parts.append(rng.choice(np.frombuffer(b"ACGTacgtN", np.uint8), int(rng.integers(0, 90))).tobytes() + b"\n")
+        text = b"".join(parts)
+        if text and rng.random() < 0.5:
+            text = text[:-1]  # no final newline
+        p = tmp_path / f"f{fi}.fa"
+        p.write_bytes(text)
+        files.append(str(p))
+        want += text + (b"\n" if text and not text.endswith(b"\n") else b"")
+    got = _pieces(files, piece_bytes)
+    assert b"".join(got) == want
+    for i, piece in enumerate(got):
+        if i > 0:
+            assert piece.startswith(b">")
+        if i < len(got) - 1:
+            assert len(piece) >= piece_bytes and piece.endswith(b"\n")
+            assert piece.find(b"\n>", max(0, piece_bytes - 1)) in (-1, len(piece) - 1)
+
+
+def test_fasta_header_names_like_the_reference():
+    """`iss >> name` on the header line after '>': leading blanks skipped, the name ends at
+    the first blank (space, tab, CR); an empty header gives an empty name."""
+    L = C.CDLL(os.path.join(ROOT, "blamm_gb300", "_build", "libblamm_host.so"))
+    L.blamm_fasta_header_name.argtypes = [C.c_char_p, C.c_int64, C.c_int64, C.c_char_p, C.c_int]
+    text = b">chr1 desc\nACGT\n>  \tchr2\tx\r\n>\n>chr3\r\nAC\n>last"
+    pos = [i for i in range(len(text)) if text[i:i + 1] == b">" and (i == 0 or text[i - 1:i] == b"\n")]
+    out = C.create_string_buffer(64)
+    names = []
+    for p in pos:
+        n = L.blamm_fasta_header_name(text, len(text), p, out, 64)
+        assert n >= 0
+        names.append(out.value.decode())
+    assert names == ["chr1", "chr2", "", "chr3", "last"]
