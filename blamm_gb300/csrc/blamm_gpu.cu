@@ -1561,23 +1561,15 @@ int blamm_set_softmask(blamm_ctx *ctx, int lowercase_scores)
     return BLAMM_OK;
 }
 
-int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
-                           int64_t nruns, const float *min_score, const float *width, int nbins,
-                           uint64_t *counts)
+// The empirical histograms of n bases already on the device (run starts on the host).
+static int score_histograms_on(blamm_ctx *ctx, const char *d_bases, int64_t n, const int64_t *run_start,
+                               int64_t nruns, const float *min_score, const float *width, int nbins,
+                               uint64_t *counts)
 {
-    const NvtxRange nvtx_range("blamm_score_histograms");
-    if (!ctx || n < 0 || nbins <= 0 || !min_score || !width || !counts) return BLAMM_ERR_ARG;
-    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
-    if (n == 0) return BLAMM_OK;
-    if (!bases || !run_start || nruns <= 0) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
-    CK(cudaSetDevice(ctx->device));
-    int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
+    int rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, (size_t)nruns);
     if (rc) return rc;
-    rc = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, (size_t)nruns);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->d_bases, bases, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_runs, run_start, sizeof(int64_t) * nruns, cudaMemcpyHostToDevice, ctx->stream));
-    rc = launch_pack(ctx, ctx->d_bases, n);
+    rc = launch_pack(ctx, d_bases, n);
     if (rc) return rc;
     const size_t nc = (size_t)ctx->ncols;
     float *d_min = nullptr, *d_w = nullptr;
@@ -1637,6 +1629,42 @@ int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const i
     if (e != cudaSuccess) return fail(ctx, BLAMM_ERR_CUDA, "%s", cudaGetErrorString(e));
     for (size_t i = 0; i < nc * (size_t)nbins; ++i) counts[i] += host[i];
     return BLAMM_OK;
+}
+
+int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
+                           int64_t nruns, const float *min_score, const float *width, int nbins,
+                           uint64_t *counts)
+{
+    const NvtxRange nvtx_range("blamm_score_histograms");
+    if (!ctx || n < 0 || nbins <= 0 || !min_score || !width || !counts) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    if (n == 0) return BLAMM_OK;
+    if (!bases || !run_start || nruns <= 0) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure(ctx, &ctx->d_bases, &ctx->cap_bases, (size_t)n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_bases, bases, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    return score_histograms_on(ctx, ctx->d_bases, n, run_start, nruns, min_score, width, nbins, counts);
+}
+
+int blamm_score_histograms_stream(blamm_ctx *ctx, int64_t begin, int64_t n, const int64_t *run_start,
+                                  int64_t nruns, const float *min_score, const float *width, int nbins,
+                                  uint64_t *counts)
+{
+    const NvtxRange nvtx_range("blamm_score_histograms_stream");
+    if (!ctx || n < 0 || begin < 0 || nbins <= 0 || !min_score || !width || !counts) return BLAMM_ERR_ARG;
+    if (ctx->ncols == 0) return fail(ctx, BLAMM_ERR_STATE, "no motif bank");
+    if (begin > ctx->stream_n || n > ctx->stream_n - begin)
+        return fail(ctx, BLAMM_ERR_ARG, "positions [%lld, %lld) outside the resident stream of %lld bases",
+                    (long long)begin, (long long)(begin + n), (long long)ctx->stream_n);
+    if (n == 0) return BLAMM_OK;
+    if (!run_start || nruns <= 0) return fail(ctx, BLAMM_ERR_ARG, "null buffer");
+    if (run_start[0] != 0) return fail(ctx, BLAMM_ERR_ARG, "run_start[0] must be 0");
+    for (int64_t r = 1; r < nruns; ++r)
+        if (run_start[r] <= run_start[r - 1] || run_start[r] >= n)
+            return fail(ctx, BLAMM_ERR_ARG, "run_start must ascend strictly inside [0, n)");
+    CK(cudaSetDevice(ctx->device));
+    return score_histograms_on(ctx, ctx->d_stream + begin, n, run_start, nruns, min_score, width, nbins, counts);
 }
 
 int blamm_debug_stall(blamm_ctx *ctx, int enable, long long wait_limit_cycles)

@@ -382,16 +382,40 @@ void empiricalHistograms(const Species &species, MotifContainer &motifs, size_t 
     check(ctx, blamm_set_motifs(ctx, motifs.matrix().data(), (int)motifs.matrixRows(), (int)motifs.size(),
                                 lens.data(), thr.data()),
           "blamm_set_motifs");
-    FastaStream fs(species.sequenceFilenames(), (int64_t)maxLength);
-    StreamChunk chunk;
-    const int64_t all = (int64_t)maxLength + 1;
-    if (!fs.nextChunk(chunk, all, 0)) return;
     const size_t nbins = hists[0].numBins();
     std::vector<uint64_t> counts(motifs.size() * nbins, 0);
-    const std::vector<int64_t> runs = chunk.runStarts();
-    check(ctx, blamm_score_histograms(ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
-                                      (int64_t)runs.size(), mn.data(), w.data(), (int)nbins, counts.data()),
-          "blamm_score_histograms");
+    if (gpuFastaReader()) {
+        // the first maxLength bases of the stream, piece by piece on the device (no window
+        // crosses a piece: pieces end where a sequence does)
+        FastaPieceReader rd(species.sequenceFilenames(), ingestPieceBytes());
+        std::string piece;
+        int64_t left = (int64_t)maxLength;
+        while (left > 0 && rd.next(piece)) {
+            int64_t nb = 0, nr = 0, ns = 0;
+            check(ctx, blamm_stream_load_fasta(ctx, piece.data(), (int64_t)piece.size(), &nb, &nr, &ns, nullptr),
+                  "blamm_stream_load_fasta");
+            std::vector<int64_t> rs((size_t)nr);
+            check(ctx, blamm_stream_tables(ctx, rs.data(), nullptr, nullptr, nullptr), "blamm_stream_tables");
+            nb = std::min(nb, left);
+            left -= nb;
+            if (nb == 0) continue;
+            std::vector<int64_t> runs;
+            for (const int64_t r : rs)
+                if (r < nb) runs.push_back(r);
+            check(ctx, blamm_score_histograms_stream(ctx, 0, nb, runs.data(), (int64_t)runs.size(), mn.data(),
+                                                     w.data(), (int)nbins, counts.data()),
+                  "blamm_score_histograms_stream");
+        }
+    } else {
+        FastaStream fs(species.sequenceFilenames(), (int64_t)maxLength);
+        StreamChunk chunk;
+        const int64_t all = (int64_t)maxLength + 1;
+        if (!fs.nextChunk(chunk, all, 0)) return;
+        const std::vector<int64_t> runs = chunk.runStarts();
+        check(ctx, blamm_score_histograms(ctx, chunk.bases.data(), (int64_t)chunk.bases.size(), runs.data(),
+                                          (int64_t)runs.size(), mn.data(), w.data(), (int)nbins, counts.data()),
+              "blamm_score_histograms");
+    }
     for (size_t c = 0; c < motifs.size(); ++c)
         for (size_t b = 0; b < nbins; ++b) hists[c].counts()[b] += counts[c * nbins + b];
 }

@@ -274,6 +274,11 @@ int blamm_set_softmask(blamm_ctx *ctx, int lowercase_scores);
 int blamm_score_histograms(blamm_ctx *ctx, const char *bases, int64_t n, const int64_t *run_start,
                            int64_t nruns, const float *min_score, const float *width, int nbins,
                            uint64_t *counts);
+/* The same over positions [begin, begin + n) of the resident stream
+ * (blamm_stream_load_fasta); run_start (host) relative to begin, run_start[0] == 0. */
+int blamm_score_histograms_stream(blamm_ctx *ctx, int64_t begin, int64_t n, const int64_t *run_start,
+                                  int64_t nruns, const float *min_score, const float *width, int nbins,
+                                  uint64_t *counts);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events around the library's. */

@@ -66,8 +66,9 @@ def test_gpu_and_host_fasta_readers_write_the_same_files(tmp_path, kind, arg, pi
     """The default FASTA reader (the text parsed on the GPU in pieces cut at header lines,
     kept on the device and scanned there) and the host reader (FastaStream, which the CPU
     suite pins to the reference's `dict` output on these cases) write byte-identical .dict,
-    hist, PWMthresholds.txt and occurrence files.  Pieces of 1 byte put every sequence in a
-    piece of its own; chunks of 5000 bases cut the pieces further."""
+    hist (theoretical and `hist -e`), PWMthresholds.txt and occurrence files.  Pieces of 1
+    byte put every sequence in a piece of its own; chunks of 5000 bases cut the pieces
+    further."""
     import os
     import subprocess
 
@@ -78,13 +79,20 @@ def test_gpu_and_host_fasta_readers_write_the_same_files(tmp_path, kind, arg, pi
                       ("gpu", {"BLAMM_INGEST_PIECE_BYTES": piece, "BLAMM_CHUNK_BASES": "5000"})):
         d = tmp_path / name
         d.mkdir()
-        for cmd in make(d, arg):
+        (d / "emp").mkdir()
+        cmds = make(d, arg)
+        mfile = next(c for c in cmds if c[0] == "hist")[-2]
+        # empirical histograms of the first 9,000 bases: the limit falls inside a piece
+        cmds.append(["hist", "-e", "-l", "9000", "-H", "emp", mfile, "sequences.mf"])
+        for cmd in cmds:
             r = subprocess.run([CLI_PATH] + cmd, cwd=d, capture_output=True, text=True,
                                env=dict(os.environ, **env))
             assert r.returncode == 0, (name, cmd, r.stderr[-800:])
         outs[name] = d
     files = sorted(p.name for p in outs["host"].iterdir() if p.is_file())
+    files += sorted("emp/" + p.name for p in (outs["host"] / "emp").iterdir())
     assert "sequences.mf.dict" in files and any(f.startswith("occ_") for f in files)
+    assert any(f.startswith("emp/hist_") for f in files)
     for f in files:
         assert (outs["host"] / f).read_bytes() == (outs["gpu"] / f).read_bytes(), f
 
